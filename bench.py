@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 thermal Monte Carlo (pdspy Model.run_thermal, code="gb300").
+
+Workload (default): 64 MCMC-walker power-law disks in one batched plan, 1e6 photon
+packets per model, parameters drawn from a seed (Mdisk log-uniform 1e-5..1e-2 Msun, Rout
+20..300 au, h0 0.03..0.2, flaring 1.0..1.3, surface-density index 0..1.5, nr 64..256,
+ntheta 64..192), small-grain dust with HG scattering, modified random walk on with
+pdspy's production settings (gamma 2, tauthres 10, count trigger 100).  Synthetic
+inputs, built in memory.
+
+A step is one full thermal run of the batch (all epochs, the continuation launch and the
+temperature inversion).  ``value`` is packets/s with densities resident in HBM; ``e2e`` is
+the same through the public API with host arrays: pinned H2D of the densities, the run,
+D2H of the temperatures.  The reference arm (``--impl reference``) times the CPU
+restatement of the same algorithm (the reference's own path is the external RADMC-3D
+binary, which is not available) on a bounded sample of the workload.
+
+With torchrun (N > 1) every rank runs its own independent batch of walkers (the models
+shard with no data-path collective): weak scaling, value = all ranks' packets / max time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MRW = dict(mrw=True, mrw_gamma=2.0, mrw_tauthres=10.0, mrw_count_trigger=100)
+METRIC = "packets/s batched vs plain GPU at <=1% median dT/T; adjoint grads/s; host CPU"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "plain"],
+                    help="batched walkers (default) or one small disk (plain)")
+    ap.add_argument("--models", type=int, default=64)
+    ap.add_argument("--packets", type=int, default=1000000, help="packets per model")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-models", type=int, default=8)
+    ap.add_argument("--cpu-packets", type=int, default=100000)
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self.loop, daemon=True)
+
+    def loop(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for n, v in zip(names, s[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def build_models(args, rank):
+    from pdspy_gb300 import workloads
+    if args.workload == "plain":
+        args.models = 1
+        return [workloads.small_disk()]
+    return workloads.walker_models(n=args.models, seed=args.seed + 1000 * rank)
+
+
+def cpu_sample(models, args, threads):
+    """The CPU restatement on the first cpu-models walkers at cpu-packets packets each."""
+    from oracle import orc  # noqa: F401  (CPU baseline leg only)
+    from tests import _cases
+    t0 = time.time()
+    pk = 0
+    nm = min(args.cpu_models, len(models))
+    for i, m in enumerate(models[:nm]):
+        _cases.run_oracle(m, args.cpu_packets, seed=args.seed, model_id=i, nthreads=threads,
+                          **MRW)
+        pk += args.cpu_packets
+    dt = time.time() - t0
+    return pk / dt, dt
+
+
+def workload_name(args):
+    if args.workload == "plain":
+        return "plain-disk-100x100-%g-packets-mrw" % args.packets
+    return "batched-%d-walker-disks-%g-packets-each-mrw" % (args.models, args.packets)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count()
+    models = build_models(args, 0)
+    for _ in range(args.warmup):
+        cpu_sample(models, args, threads)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, dt = cpu_sample(models, args, threads)
+        vals.append(v)
+        times.append(dt)
+    value = float(np.sum([args.cpu_models * args.cpu_packets] * args.steps) / np.sum(times))
+    sample = "%d walkers x %d packets (of the %d x %g workload), CPU restatement, %d threads" % (
+        args.cpu_models, args.cpu_packets, args.models, args.packets, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "packets/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(times) * 1e3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": workload_name(args), "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "packets/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "packets/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+    import torch.distributed as dist
+    from pdspy_gb300 import thermal
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    models = build_models(args, rank)
+    plan = thermal.ThermalPlan([m.grid for m in models], args.packets, seed=args.seed,
+                               time_launches=True, **MRW)
+    host_rho = torch.from_numpy(np.concatenate(
+        [thermal.stack_density(m.grid).reshape(-1) for m in models])).pin_memory()
+    rho, T = plan.new_buffers()
+    rho.copy_(host_rho)
+    host_T = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+    total_packets = args.models * args.packets
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        plan.run(rho, T)
+    plan.check_status()
+
+    # device-resident timing
+    step_ms, launch_ms, stats = [], [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            barrier()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            plan.run(rho, T)
+            b.record(stream)
+            barrier()
+            step_ms.append(a.elapsed_time(b))
+            launch_ms.append(plan.launch_ms())
+            stats.append(plan.check_status())
+    t_local = float(np.sum(step_ms))
+    t_max = t_local
+    if world > 1:
+        tt = torch.tensor([t_local], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * total_packets * args.steps / (t_max / 1e3)
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e_ms = []
+        for i in range(args.steps):
+            flush.zero_()
+            barrier()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            rho.copy_(host_rho, non_blocking=True)
+            plan.run(rho, T)
+            host_T.copy_(T, non_blocking=True)
+            b.record(stream)
+            barrier()
+            e_ms.append(a.elapsed_time(b))
+        te = float(np.sum(e_ms))
+        if world > 1:
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": world * total_packets * args.steps / (te / 1e3), "unit": "packets/s",
+               "h2d_bytes_per_step": int(host_rho.numel() * 4),
+               "d2h_bytes_per_step": int(host_T.numel() * 8)}
+
+    # roofline of the dominant kernel (the transport launches)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    st = stats[-1]
+    ns = plan.nspec
+    alg_bytes = (st["crossings"] * 4 * ns + (st["absorptions"] + st["mrw_steps"] * ns) * 8 +
+                 (st["absorptions"] + st["mrw_steps"]) * 4)
+    lm = [x for x in launch_ms[-1] if x > 0]
+    n_launch = max(len(lm), 1)
+    avg_launch = float(np.sum(lm)) / n_launch
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "mc_transport_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    achieved = (alg_bytes / n_launch) / (avg_launch / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "mc_transport_kernel", "peak_source": "measured" if peaks else "fallback",
+                "launches_per_step": n_launch, "kernel_ms_per_step": float(np.sum(lm)),
+                "algorithmic_bytes_per_step": int(alg_bytes)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, dt = cpu_sample(models, args, os.cpu_count())
+        cpu = {"value": v, "unit": "packets/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "%d walkers x %d packets of the workload, CPU restatement (%.1f s)" %
+               (args.cpu_models, args.cpu_packets, dt)}
+
+    K, P = plan.opts.nepoch, plan.opts.npilot
+    launches_per_step = 2 * (st["launches"]) - 1 + 3
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": workload_name(args), "models_per_gpu": args.models,
+                           "packets_per_model": args.packets, "mrw": True, "nepoch": K,
+                           "npilot": P, "late_after": int(plan.opts.late_after),
+                           "l2": "256 MB buffer written between timed steps",
+                           "parallelism": "replicas: independent walker batches per GPU"},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+                "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
+                                            "parked", "killed")},
+                "launch_ms": [round(x, 3) for x in launch_ms[-1]]}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

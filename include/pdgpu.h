@@ -1,0 +1,179 @@
+/*
+ * pdgpu: GB300 (sm_103a) backend for pdspy's radiative-transfer hot path.
+ *
+ * C ABI: plain pointers and sizes, no C++ or torch types.  Every entry point replaces a
+ * step of pdspy's radmc3d branch, which today serialises the model to ASCII files, runs
+ * the external RADMC-3D binary in a subprocess and parses its output files:
+ *
+ *   pdgpu_mc_*          Model.run_thermal -> run_thermal_radmc3d
+ *                       (pdspy/modeling/Model.py:54-72, :221-256): write_radmc3d
+ *                       (Model.py:723-825, radmc3d/write.py:1-342), radmc3d.run.thermal
+ *                       (radmc3d/run.py:9-38), radmc3d.read.dust_temperature
+ *                       (radmc3d/read.pyx:433-478) and the reshape at Model.py:250-254.
+ *   pdgpu_image*        Model.run_image -> run_image_radmc3d (Model.py:324-348,
+ *                       :515-577): radmc3d.run.image (radmc3d/run.py:157-289) and
+ *                       radmc3d.read.image (radmc3d/read.pyx:25-152).
+ *   pdgpu_image_adjoint reverse-mode derivative of the same ray trace; no counterpart in
+ *                       the reference (pdspy fits by sampling, utils/emcee.py:6-61).
+ *   pdgpu_vis_*         direct Fourier transform of an image at uv points and the chi^2
+ *                       of interferometry/libinterferometry.pyx:610-633 (chisq_calc).
+ *
+ * Conventions.  Arrays marked "device" are caller-owned device buffers; arrays marked
+ * "host" are read during the call only.  Cell arrays use numpy's C order of pdspy's
+ * (nr, ntheta, nphi) grids (pdspy/modeling/Grid.py:71-80); species are stacked in front
+ * ([nspec][nr][ntheta][nphi]) and models in front of species for batched plans.  Radii
+ * are in cm (pdspy multiplies grid.w1 by AU at Model.py:754-756), angles in radians,
+ * wavelengths in microns, opacities in cm^2/g, temperatures in K.
+ *
+ * Errors are returned as pdgpu_status; no exception crosses the ABI.  Entry points
+ * allocate no device memory: the caller passes a workspace of the queried size.
+ * Calls on different plans and streams are independent; a plan must not be run on two
+ * streams at once.
+ */
+#ifndef PDGPU_H
+#define PDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDGPU_ABI_VERSION 1
+
+typedef int32_t pdgpu_status;
+enum {
+    PDGPU_OK = 0,
+    PDGPU_INVALID_ARG = 1,   /* bad sizes, grid not spherical [0,pi] or [0,pi/2], ...   */
+    PDGPU_TIMEOUT = 2,       /* deadline_ns elapsed; mirrors radmc3d's timelimit        */
+    PDGPU_ABORTED = 3,       /* the abort flag was raised by the host                   */
+    PDGPU_PACKET_CAP = 4,    /* informational: packets hit max_interactions             */
+    PDGPU_OVERFLOW = 5,      /* a fixed-point accumulator would overflow                */
+    PDGPU_CUDA_ERROR = 6,    /* a CUDA runtime call failed                              */
+    PDGPU_NO_DEVICE = 7,     /* no usable sm_103 device                                 */
+    PDGPU_WORKSPACE = 8      /* workspace missing, too small or not uploaded            */
+};
+
+/* Library identity. Replaces nothing in the reference (version probe for the binding). */
+int32_t pdgpu_abi_version(void);
+const char* pdgpu_status_string(pdgpu_status status);
+
+/* ------------------------------------------------------------------------- */
+/* Thermal Monte Carlo (Model.run_thermal)                                    */
+/* ------------------------------------------------------------------------- */
+
+/* One model: its spherical grid, its stars and its packet count.
+ * Replaces write.amr_grid (radmc3d/write.py:198-244), write.stars (:148-172) and the
+ * nphot_therm keyword of write.control (:31-32). */
+typedef struct {
+    int32_t nr, ntheta, nphi;
+    const double* r_edges_cm;       /* host [nr+1], r_edges_cm[0] > 0                  */
+    const double* theta_edges;      /* host [ntheta+1]: 0..pi, or 0..pi/2 (mirrored)    */
+    const double* phi_edges;        /* host [nphi+1]: 0..2 pi                           */
+    int32_t nstar;                  /* blackbody point stars at the origin              */
+    const double* star_radius_cm;   /* host [nstar]                                     */
+    const double* star_temperature; /* host [nstar], K                                  */
+    int64_t nphot;                  /* photon packets for this model                    */
+} pdgpu_model_desc;
+
+/* Dust opacities of every species on the shared wavelength grid.
+ * Replaces write.wavelength_micron (radmc3d/write.py:174-184), write.dustkappa
+ * (:316-342) and write.dustopac (:290-314).  g may be NULL (isotropic scattering, which
+ * is what pdspy's iformat-2 dustkappa files give RADMC-3D). */
+typedef struct {
+    int32_t nlam, nspec;
+    const double* lam_um;           /* host [nlam], ascending                           */
+    const double* kabs;             /* host [nspec][nlam]                               */
+    const double* ksca;             /* host [nspec][nlam]                               */
+    const double* g;                /* host [nspec][nlam] or NULL                       */
+} pdgpu_dust_desc;
+
+/* Run controls.  Replaces the thermal keywords of write.control
+ * (radmc3d/write.py:1-146: iseed, modified_random_walk, mrw_gamma, mrw_tauthres,
+ * mrw_count_trigger) and run.thermal's timelimit (radmc3d/run.py:9-38). */
+typedef struct {
+    uint64_t seed;
+    int32_t nepoch;                 /* B&W epochs with doubling sizes (default 8)       */
+    int32_t npilot;                 /* pilot passes of the first epoch (default 2)      */
+    int32_t mrw;                    /* modified random walk on/off                      */
+    float mrw_gamma;
+    float mrw_tauthres;
+    int32_t mrw_count_trigger;
+    int64_t max_interactions;       /* per-packet event cap (killed and counted)        */
+    int64_t deadline_ns;            /* device-clock budget for one run, 0 = none        */
+    const volatile int32_t* abort_flag; /* device-readable (e.g. host-mapped) or NULL    */
+    int32_t block_threads;          /* 0 = default; schedule knobs for the autotuner    */
+    int32_t blocks_per_sm;          /* 0 = as many as fit                               */
+    int64_t late_after;             /* events of a packet that feed later epochs'       */
+                                    /* temperatures; later ones count at the end (0=all)*/
+    int32_t time_launches;          /* 1: record CUDA events around transport launches  */
+    int64_t mrw_eager_after;        /* beyond this many events of a packet MRW is tried */
+                                    /* at every event (0 = never)                       */
+} pdgpu_mc_options;
+
+typedef struct {
+    int64_t packets, killed, escaped, crossings, events, absorptions, scatterings,
+        mrw_steps;
+    int32_t status;                 /* pdgpu_status reached by the device               */
+    int32_t launches;               /* transport launches of the last run               */
+    int64_t parked;                 /* packets resumed by the continuation launch       */
+    int64_t late_units;             /* energy deposited after late_after events         */
+} pdgpu_mc_stats;
+
+/* Byte offsets of the run's device arrays inside the workspace. */
+typedef struct {
+    size_t tables_bytes;            /* constant tables written by plan_upload           */
+    size_t energy_offset;           /* int64 [total_cells] absorbed energy, 2^-20 packets */
+    size_t late_offset;             /* int64 [total_cells] energy absorbed after        */
+                                    /* late_after events of a packet                     */
+    size_t escape_offset;           /* int64 [nmodels][nlam] escaping packets per bin    */
+    size_t stats_offset;            /* int64 [64]: counters, then per launch             */
+                                    /* (t_start, t_end, max events, parked) from slot 32 */
+    size_t total_bytes;
+    int64_t total_cells;            /* sum over models of nspec * ncell                  */
+    int32_t nmodels, nspec, nlam;
+    int32_t smem_tables;            /* 1 when the tables fit in shared memory            */
+} pdgpu_mc_layout;
+
+typedef struct pdgpu_mc_plan pdgpu_mc_plan;
+
+/* Prepare one or more models sharing one dust description (host work only: tables,
+ * wall geometry, epoch schedule).  nmodels > 1 gives the batched persistent launch. */
+pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* models,
+                                  const pdgpu_dust_desc* dust,
+                                  const pdgpu_mc_options* options, pdgpu_mc_plan** plan);
+void pdgpu_mc_plan_destroy(pdgpu_mc_plan* plan);
+pdgpu_status pdgpu_mc_plan_layout(const pdgpu_mc_plan* plan, pdgpu_mc_layout* layout);
+
+/* Copy the plan's constant tables into the workspace (stream-ordered H2D). */
+pdgpu_status pdgpu_mc_plan_upload(pdgpu_mc_plan* plan, void* workspace, size_t bytes,
+                                  void* stream);
+
+/* Enqueue one thermal run: rho (device float [models][nspec][cells]) in, temperature
+ * (device double, same layout) out.  Only kernel launches and memsets are enqueued, so
+ * the call can be captured into a CUDA graph and replayed. */
+pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* plan, const float* rho, double* temperature,
+                               void* workspace, size_t bytes, void* stream);
+
+/* Synchronise the stream and read the run's counters and device status. */
+/* Durations (ms, CUDA events on the run's stream) of the transport launches of the last
+ * run when options.time_launches was set; returns the number written (<= capacity). */
+int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* plan, float* ms, int32_t capacity);
+
+pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* plan, const void* workspace, void* stream,
+                                 pdgpu_mc_stats* stats);
+
+/* One-shot convenience: create, upload, run, read stats, destroy. */
+pdgpu_status pdgpu_mctherm(int32_t nmodels, const pdgpu_model_desc* models,
+                           const pdgpu_dust_desc* dust, const pdgpu_mc_options* options,
+                           const float* rho, double* temperature, void* workspace,
+                           size_t bytes, void* stream, pdgpu_mc_stats* stats);
+size_t pdgpu_mctherm_workspace_bytes(int32_t nmodels, const pdgpu_model_desc* models,
+                                     const pdgpu_dust_desc* dust,
+                                     const pdgpu_mc_options* options);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

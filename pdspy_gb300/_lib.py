@@ -1,0 +1,116 @@
+"""ctypes binding of the C ABI declared in include/pdgpu.h.
+
+The library is built in-tree (``pdspy_gb300/_build/libpdgpu.so``).  Loading fails loudly
+when it is missing: there is no CPU fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+from . import _build
+
+_lib = None
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [("nr", C.c_int32), ("ntheta", C.c_int32), ("nphi", C.c_int32),
+                ("r_edges_cm", C.POINTER(C.c_double)), ("theta_edges", C.POINTER(C.c_double)),
+                ("phi_edges", C.POINTER(C.c_double)), ("nstar", C.c_int32),
+                ("star_radius_cm", C.POINTER(C.c_double)),
+                ("star_temperature", C.POINTER(C.c_double)), ("nphot", C.c_int64)]
+
+
+class DustDesc(C.Structure):
+    _fields_ = [("nlam", C.c_int32), ("nspec", C.c_int32), ("lam_um", C.POINTER(C.c_double)),
+                ("kabs", C.POINTER(C.c_double)), ("ksca", C.POINTER(C.c_double)),
+                ("g", C.POINTER(C.c_double))]
+
+
+class McOptions(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("nepoch", C.c_int32), ("npilot", C.c_int32),
+                ("mrw", C.c_int32), ("mrw_gamma", C.c_float), ("mrw_tauthres", C.c_float),
+                ("mrw_count_trigger", C.c_int32), ("max_interactions", C.c_int64),
+                ("deadline_ns", C.c_int64), ("abort_flag", C.c_void_p),
+                ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("late_after", C.c_int64), ("time_launches", C.c_int32),
+                ("mrw_eager_after", C.c_int64)]
+
+
+class McStats(C.Structure):
+    _fields_ = [("packets", C.c_int64), ("killed", C.c_int64), ("escaped", C.c_int64),
+                ("crossings", C.c_int64), ("events", C.c_int64), ("absorptions", C.c_int64),
+                ("scatterings", C.c_int64), ("mrw_steps", C.c_int64), ("status", C.c_int32),
+                ("launches", C.c_int32), ("parked", C.c_int64), ("late_units", C.c_int64)]
+
+    def asdict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class McLayout(C.Structure):
+    _fields_ = [("tables_bytes", C.c_size_t), ("energy_offset", C.c_size_t),
+                ("late_offset", C.c_size_t), ("escape_offset", C.c_size_t), ("stats_offset", C.c_size_t),
+                ("total_bytes", C.c_size_t), ("total_cells", C.c_int64),
+                ("nmodels", C.c_int32), ("nspec", C.c_int32), ("nlam", C.c_int32),
+                ("smem_tables", C.c_int32)]
+
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "time limit reached", 3: "aborted",
+          4: "packet cap", 5: "overflow", 6: "CUDA error", 7: "no device", 8: "workspace"}
+
+# Every symbol include/pdgpu.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "pdgpu_abi_version", "pdgpu_status_string",
+    "pdgpu_mc_plan_create", "pdgpu_mc_plan_destroy", "pdgpu_mc_plan_layout",
+    "pdgpu_mc_plan_upload", "pdgpu_mc_plan_run", "pdgpu_mc_plan_stats",
+    "pdgpu_mctherm", "pdgpu_mctherm_workspace_bytes", "pdgpu_mc_plan_launch_ms",
+]
+
+
+class PdgpuError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = int(status)
+        super().__init__("%s: %s (status %d)" % (what, STATUS.get(self.status, "?"), self.status))
+
+
+def lib(build_if_missing=True):
+    """Load (building first if needed) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("pdspy_gb300 CUDA library missing at %s; run build()" % path)
+    L = C.CDLL(path)
+    vp, i32, sz = C.c_void_p, C.c_int32, C.c_size_t
+    L.pdgpu_abi_version.restype = i32
+    L.pdgpu_status_string.restype = C.c_char_p
+    L.pdgpu_status_string.argtypes = [i32]
+    L.pdgpu_mc_plan_create.restype = i32
+    L.pdgpu_mc_plan_create.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
+                                       C.POINTER(McOptions), C.POINTER(vp)]
+    L.pdgpu_mc_plan_destroy.restype = None
+    L.pdgpu_mc_plan_destroy.argtypes = [vp]
+    L.pdgpu_mc_plan_layout.restype = i32
+    L.pdgpu_mc_plan_layout.argtypes = [vp, C.POINTER(McLayout)]
+    L.pdgpu_mc_plan_upload.restype = i32
+    L.pdgpu_mc_plan_upload.argtypes = [vp, vp, sz, vp]
+    L.pdgpu_mc_plan_run.restype = i32
+    L.pdgpu_mc_plan_run.argtypes = [vp, vp, vp, vp, sz, vp]
+    L.pdgpu_mc_plan_stats.restype = i32
+    L.pdgpu_mc_plan_stats.argtypes = [vp, vp, vp, C.POINTER(McStats)]
+    L.pdgpu_mc_plan_launch_ms.restype = i32
+    L.pdgpu_mc_plan_launch_ms.argtypes = [vp, C.POINTER(C.c_float), i32]
+    L.pdgpu_mctherm.restype = i32
+    L.pdgpu_mctherm.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
+                                C.POINTER(McOptions), vp, vp, vp, sz, vp, C.POINTER(McStats)]
+    L.pdgpu_mctherm_workspace_bytes.restype = sz
+    L.pdgpu_mctherm_workspace_bytes.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
+                                                C.POINTER(McOptions)]
+    _lib = L
+    return L
+
+
+def check(status, what):
+    if status != 0:
+        raise PdgpuError(status, what)

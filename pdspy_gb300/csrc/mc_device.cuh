@@ -1,0 +1,160 @@
+// Device building blocks of the thermal Monte Carlo: counter-based random numbers,
+// the single-precision math the walk uses, direction sampling and table searches.
+//
+// Every expression is written out operation by operation and the translation unit is
+// compiled with --fmad=false, so that each floating-point operation is one IEEE
+// operation.  The CPU oracle evaluates the same sequence, which makes a GPU run and an
+// oracle run with the same seed consume identical random numbers and take identical
+// decisions.
+#pragma once
+#include <stdint.h>
+
+#include "mc_common.h"
+
+#define PHILOX_M0 0xD2511F53u
+#define PHILOX_M1 0xCD9E8D57u
+#define PHILOX_W0 0x9E3779B9u
+#define PHILOX_W1 0xBB67AE85u
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t lo0 = PHILOX_M0 * c.x;
+        uint32_t hi0 = __umulhi(PHILOX_M0, c.x);
+        uint32_t lo1 = PHILOX_M1 * c.z;
+        uint32_t hi1 = __umulhi(PHILOX_M1, c.z);
+        uint4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+        k0 += PHILOX_W0;
+        k1 += PHILOX_W1;
+    }
+    return c;
+}
+
+// Uniform in (0,1): 23 random bits as an odd multiple of 2^-24 (exact in float).
+__device__ __forceinline__ float mc_u01(uint32_t x) {
+    return (float)(((x >> 9) << 1) | 1u) * 5.9604644775390625e-08f;
+}
+
+// ln(x) for normal positive floats: x = 2^e m with m in (sqrt(1/2), sqrt(2)];
+// ln m = 2 atanh(t), t = (m-1)/(m+1), by the atanh power series to t^9.
+__device__ __forceinline__ float mc_logf(float x) {
+    uint32_t bits = __float_as_uint(x);
+    int e = (int)((bits >> 23) & 0xffu) - 127;
+    float m = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e = e + 1;
+    }
+    float t = (m - 1.0f) / (m + 1.0f);
+    float s = t * t;
+    float p = 0.11111111f;
+    p = p * s + 0.14285715f;
+    p = p * s + 0.2f;
+    p = p * s + 0.33333334f;
+    float t2 = 2.0f * t;
+    float lm = t2 + t2 * (s * p);
+    return (float)e * 0.69314718f + lm;
+}
+
+// sin and cos of 2 pi u, u in (0,1): nearest quarter turn plus Taylor series of sin (to
+// x^9) and cos (to x^8) on |x| <= pi/4.
+__device__ __forceinline__ void mc_sincospif2(float u, float& sn, float& cs) {
+    float a = 2.0f * u;
+    int n = (int)(a * 2.0f + 0.5f);
+    float r = a - (float)n * 0.5f;
+    float x = r * 3.14159265f;
+    float x2 = x * x;
+    float sp = 2.7557319e-06f;
+    sp = sp * x2 - 1.9841270e-04f;
+    sp = sp * x2 + 8.3333333e-03f;
+    sp = sp * x2 - 1.6666667e-01f;
+    float sx = x + x * (x2 * sp);
+    float cp = 2.4801587e-05f;
+    cp = cp * x2 - 1.3888889e-03f;
+    cp = cp * x2 + 4.1666668e-02f;
+    cp = cp * x2 - 0.5f;
+    float cx = 1.0f + x2 * cp;
+    switch (n & 3) {
+        case 0: sn = sx; cs = cx; break;
+        case 1: sn = cx; cs = -sx; break;
+        case 2: sn = -sx; cs = -cx; break;
+        default: sn = -cx; cs = sx; break;
+    }
+}
+
+// Per-packet random stream: counter (block, packet, model, pass tag), key = seed.
+struct McRng {
+    uint32_t pid, model, tag, draw;
+    uint32_t b0, b1, b2, b3;
+};
+
+__device__ __forceinline__ float mc_next(McRng& r, uint32_t k0, uint32_t k1) {
+    uint32_t i = r.draw & 3u;
+    if (i == 0u) {
+        uint4 o = philox4x32_10(make_uint4(r.draw >> 2, r.pid, r.model, r.tag), k0, k1);
+        r.b0 = o.x; r.b1 = o.y; r.b2 = o.z; r.b3 = o.w;
+    }
+    r.draw += 1u;
+    uint32_t x = (i == 0u) ? r.b0 : (i == 1u) ? r.b1 : (i == 2u) ? r.b2 : r.b3;
+    return mc_u01(x);
+}
+
+// Rotate unit vector k by polar cosine mu and azimuth (cp, sp) about itself.
+__device__ __forceinline__ void mc_rotate(float& kx, float& ky, float& kz, float mu, float cp,
+                                          float sp) {
+    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+    float ax = kx, ay = ky, az = kz;
+    float nx, ny, nz;
+    float w2 = 1.0f - az * az;
+    if (w2 > 1.0e-10f) {
+        float w = sqrtf(w2);
+        nx = mu * ax + st * (ax * az * cp - ay * sp) / w;
+        ny = mu * ay + st * (ay * az * cp + ax * sp) / w;
+        nz = mu * az - st * cp * w;
+    } else {
+        nx = st * cp;
+        ny = st * sp;
+        nz = (az >= 0.0f) ? mu : -mu;
+    }
+    float n = sqrtf(nx * nx + ny * ny + nz * nz);
+    kx = nx / n;
+    ky = ny / n;
+    kz = nz / n;
+}
+
+// Smallest index l with cdf[l] > u (cdf[n-1] == 1 > u).
+__device__ __forceinline__ int mc_cdf_search(const float* cdf, int n, float u) {
+    int lo = -1, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = lo + (hi - lo) / 2;
+        if (cdf[mid] > u) hi = mid; else lo = mid;
+    }
+    return hi;
+}
+
+// Fractional reemission row of q on the increasing row table F[MC_NROW].
+__device__ __forceinline__ void mc_row_search(const float* F, float q, int& j, float& w) {
+    if (q < F[0]) {
+        j = 0;
+        w = 0.0f;
+    } else if (q >= F[MC_NROW - 1]) {
+        j = MC_NROW - 2;
+        w = 1.0f;
+    } else {
+        int lo = 0, hi = MC_NROW - 1;
+        while (hi - lo > 1) {
+            int mid = lo + (hi - lo) / 2;
+            if (F[mid] <= q) lo = mid; else hi = mid;
+        }
+        j = lo;
+        w = (q - F[j]) / (F[j + 1] - F[j]);
+        if (w < 0.0f) w = 0.0f;
+        if (w > 1.0f) w = 1.0f;
+    }
+}

@@ -1,0 +1,1483 @@
+// Thermal Monte Carlo photon transport on spherical grids (GB300, sm_103a).
+//
+// Replaces the "radmc3d mctherm" subprocess behind pdspy's Model.run_thermal
+// (pdspy/modeling/Model.py:221-256, pdspy/radmc3d/run.py:9-38).  Methods: Bjorkman &
+// Wood 2001 immediate reemission with integer energy counting, made order-independent
+// by epochs (below); the modified random walk of Min et al. 2009 / Robitaille 2010;
+// Philox4x32-10 random numbers keyed by (seed; draw block, packet, model, pass).
+//
+// Execution model.  One persistent kernel per epoch.  Each thread owns one packet at a
+// time; its whole state lives in registers (structure-of-arrays across the warp).  When
+// packets finish, the warp refills the free lanes with one warp-aggregated atomicAdd on
+// the epoch's work counter (ballot + popc + shfl), so the queue is read with one
+// atomic per refill instead of one per packet.  Models of a batched plan are
+// interleaved in the same queue.  Opacity, reemission-row, reemission-CDF and MRW tables
+// are staged in shared memory when they fit.  Absorbed energy is accumulated in int64
+// fixed point (2^20 units per packet) with atomicAdd, so the sum does not depend on the
+// order of the atomics and a run is bit-reproducible for a given seed.
+//
+// Deterministic B&W.  Packets [b_k, b_{k+1}) form epoch k; sizes double from epoch to
+// epoch.  In epoch k the reemission temperature of an absorption in cell c is taken at
+// q' = q_lo + u * q_span (energy absorbed per gram per second), with q_lo from the
+// energy absorbed in earlier epochs and q_span = q_lo (b_{k+1}/b_k - 1) its expected
+// growth over the epoch.  The first epoch runs npilot pilot passes that estimate its own
+// span.  FP64 is used for the wall-intersection root solves (and the packet position
+// they update) and for the energy -> temperature inversion; everything else is FP32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/pdgpu.h"
+#include "mc_common.h"
+#include "mc_device.cuh"
+
+namespace {
+
+enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI = 6 };
+
+// Saved state of a parked packet (everything in Pkt except the Philox buffer, which is
+// regenerated from the draw counter).
+struct __align__(16) ParkRec {
+    double x, y, z, dsafe;
+    float kx, ky, kz, tau;
+    int ir, itv, ip, lam;
+    int last_wall, cell_events, nevents, ncross;
+    int m, epoch;
+    uint32_t pid, model, tag, draw;
+    int pad[2];
+};
+
+struct DustTabs {       // pointers into the staged (shared or global) dust tables
+    const float* kabs;  // [ns][nl]
+    const float* ksca;
+    const float* kext;
+    const float* g;
+    const float* F;     // [ns][NROW]
+    const float* cdf;   // [ns][NROW][nl]
+    const float* kP;    // [ns][NROW]
+    const float* kR;
+    const float* mrw;   // [NMRW]
+};
+
+struct McParams {
+    const float* fpool;
+    const double* dpool;
+    const McModel* models;
+    const int64_t* cum;          // [nm+1] prefix of this epoch's packet counts
+    const float* rho;            // [model][spec][cell]
+    int64_t* E;                  // deposits of a packet's first late_after events
+    int64_t* Elate;              // deposits of its later events
+    const float2* q;             // (q_lo, q_span) per [epoch][model][spec][cell]
+    int64_t qstride;             // cells per epoch snapshot
+    int64_t late_after;          // 0: all deposits go to E
+    ParkRec* park;               // packets parked after late_after events
+    unsigned long long* park_count;
+    int64_t park_cap;
+    int32_t pilot;               // pilot pass: packets stop after late_after events
+    int32_t phase;               // 0: epoch launch, 1: continuation of parked packets
+    int32_t lslot;               // per-launch debug slot
+    int64_t* escape;             // [nm][nl] or null
+    int64_t* stats;              // [MC_NSTAT]
+    unsigned long long* queue;   // work counter of this launch
+    const volatile int32_t* abort_flag;
+    int64_t deadline_ns;
+    int64_t total;
+    int32_t nm, ns, nl, epoch;
+    uint32_t tag, key0, key1;
+    int32_t mrw, mrw_trigger;
+    int32_t mrw_eager_after;
+    float mrw_gamma, mrw_tauthres;
+    int32_t max_inter;
+    int32_t dust_floats, use_smem;
+    int32_t o_kabs, o_ksca, o_kext, o_g, o_F, o_cdf, o_kP, o_kR, o_mrw;
+    int32_t count_stats;
+};
+
+struct Pkt {
+    double x, y, z;
+    double dsafe;   // lower bound of the distance to every wall of the cell
+    float kx, ky, kz, tau;
+    int ir, itv, ip, lam;
+    int last_wall, cell_events;
+    int nevents, ncross;
+    int m, epoch;
+    McRng rng;
+};
+
+struct Cnt {
+    long long killed, escaped, crossings, events, absorb, scatter, mrw, late, parked;
+    int maxev;
+};
+
+__device__ __forceinline__ bool accept_root(double s, int wall, int last, double tol, double& out) {
+    if (wall == last) {
+        if (s > tol) { out = s; return true; }
+        return false;
+    }
+    if (s >= -tol) { out = s > 0.0 ? s : 0.0; return true; }
+    return false;
+}
+
+// Distance to the wall through which the packet leaves its cell (FP64 root solves).
+__device__ double next_wall(const McModel& M, const double* __restrict__ dp, const Pkt& p,
+                            int& wall_out) {
+    const double* R = dp + M.off_r;
+    double x = p.x, y = p.y, z = p.z;
+    double kx = (double)p.kx, ky = (double)p.ky, kz = (double)p.kz;
+    double kk = kx * kx + ky * ky + kz * kz;
+    double r2 = x * x + y * y + z * z;
+    double b = x * kx + y * ky + z * kz;
+    int last = p.last_wall;
+    double best = 1.0e300;
+    int bw = W_NONE;
+    double Ro = (p.ir < 0) ? R[0] : R[p.ir + 1];
+    double tol = 1.0e-10 * Ro;
+    double cand;
+    {
+        double c = r2 - Ro * Ro;
+        double D = b * b - kk * c;
+        if (D < 0.0) D = 0.0;
+        double sq = sqrt(D);
+        double s = (b <= 0.0) ? (sq - b) / kk : -c / (b + sq);
+        if (!(last == W_ROUT && s <= tol)) { best = (s > 0.0) ? s : 0.0; bw = W_ROUT; }
+    }
+    if (p.ir < 0) { wall_out = bw; return best; }
+    if (b < 0.0) {
+        double Ri = R[p.ir];
+        double c = r2 - Ri * Ri;
+        double D = b * b - kk * c;
+        if (D >= 0.0) {
+            double s = c / (sqrt(D) - b);
+            if (accept_root(s, W_RIN, last, tol, cand) && cand < best) { best = cand; bw = W_RIN; }
+        }
+    }
+    const double* MU = dp + M.off_mu;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        int w = p.itv + side;
+        if (w == 0 || w == M.ntv) continue;
+        int code = side ? W_THI : W_TLO;
+        double mu = MU[w];
+        double s = 0.0;
+        bool ok = false;
+        if (mu == 0.0) {
+            if (side == 0 ? (kz > 0.0) : (kz < 0.0)) { s = -z / kz; ok = true; }
+        } else {
+            double mu2 = mu * mu;
+            double A = kz * kz - mu2 * kk;
+            double B = z * kz - mu2 * b;
+            double C = z * z - mu2 * r2;
+            bool want_plus = (side == 0) ? (mu > 0.0) : (mu < 0.0);
+            double D = B * B - A * C;
+            if (D >= 0.0) {
+                double sq = sqrt(D);
+                if (A == 0.0) {
+                    if (want_plus ? (B > 0.0) : (B < 0.0)) { s = -C / (2.0 * B); ok = true; }
+                } else {
+                    double q = (B >= 0.0) ? -(B + sq) : (sq - B);
+                    if (q != 0.0) {
+                        double sm, sp;
+                        if (B >= 0.0) { sm = q / A; sp = C / q; }
+                        else { sp = q / A; sm = C / q; }
+                        s = want_plus ? sp : sm;
+                        ok = true;
+                    }
+                }
+                if (ok) {
+                    double zs = z + s * kz;
+                    if (mu > 0.0 ? (zs < 0.0) : (zs > 0.0)) ok = false;
+                }
+            }
+        }
+        if (ok && accept_root(s, code, last, tol, cand) && cand < best) { best = cand; bw = code; }
+    }
+    if (M.np > 1) {
+        const double* CP = dp + M.off_cph;
+        const double* SP = dp + M.off_sph;
+        int k0 = p.ip, k1 = p.ip + 1;
+        double g0 = -x * SP[k0] + y * CP[k0];
+        double dg = -kx * SP[k0] + ky * CP[k0];
+        if (dg < 0.0) {
+            double s = -g0 / dg;
+            double hx = x + s * kx, hy = y + s * ky;
+            if (hx * CP[k0] + hy * SP[k0] > 0.0 && accept_root(s, W_PLO, last, tol, cand) &&
+                cand < best) { best = cand; bw = W_PLO; }
+        }
+        double h0 = x * SP[k1] - y * CP[k1];
+        double dh = kx * SP[k1] - ky * CP[k1];
+        if (dh < 0.0) {
+            double s = -h0 / dh;
+            double hx = x + s * kx, hy = y + s * ky;
+            if (hx * CP[k1] + hy * SP[k1] > 0.0 && accept_root(s, W_PHI, last, tol, cand) &&
+                cand < best) { best = cand; bw = W_PHI; }
+        }
+    }
+    wall_out = bw;
+    return best;
+}
+
+__device__ void locate_angles(const McModel& M, const double* __restrict__ dp, Pkt& p) {
+    double x = p.x, y = p.y, z = p.z;
+    double r = sqrt(x * x + y * y + z * z);
+    double ct = z / r;
+    const double* MU = dp + M.off_mu;
+    int lo = 0, hi = M.ntv;
+    while (hi - lo > 1) {
+        int mid = lo + (hi - lo) / 2;
+        if (MU[mid] >= ct) lo = mid; else hi = mid;
+    }
+    p.itv = lo;
+    if (M.np > 1) {
+        double ph = atan2(y, x);
+        if (ph < 0.0) ph += 2.0 * MC_PI;
+        const double* PH = dp + M.off_vp + M.np;  // phi edges follow the phi widths
+        int a = 0, bnd = M.np;
+        while (bnd - a > 1) {
+            int mid = a + (bnd - a) / 2;
+            if (PH[mid] <= ph) a = mid; else bnd = mid;
+        }
+        p.ip = a;
+    } else {
+        p.ip = 0;
+    }
+}
+
+__device__ __forceinline__ int cell_of(const McModel& M, const Pkt& p) {
+    int it = (p.itv < M.nt) ? p.itv : (2 * M.nt - 1 - p.itv);
+    return (p.ir * M.nt + it) * M.np + p.ip;
+}
+
+__device__ double wall_distance(const McModel& M, const double* __restrict__ dp, const Pkt& p) {
+    const double* R = dp + M.off_r;
+    const double* MU = dp + M.off_mu;
+    const double* SN = dp + M.off_sn;
+    double x = p.x, y = p.y, z = p.z;
+    double r = sqrt(x * x + y * y + z * z);
+    double d = r - R[p.ir];
+    double d2 = R[p.ir + 1] - r;
+    if (d2 < d) d = d2;
+    double rc = sqrt(x * x + y * y);
+    for (int side = 0; side < 2; ++side) {
+        int w = p.itv + side;
+        if (w == 0 || w == M.ntv) continue;
+        double dt = fabs(rc * MU[w] - z * SN[w]);
+        if (dt < d) d = dt;
+    }
+    if (M.np > 1) {
+        const double* CP = dp + M.off_cph;
+        const double* SP = dp + M.off_sph;
+        int k0 = p.ip, k1 = p.ip + 1;
+        double d0 = fabs(-x * SP[k0] + y * CP[k0]);
+        double d1 = fabs(x * SP[k1] - y * CP[k1]);
+        if (d0 < d) d = d0;
+        if (d1 < d) d = d1;
+    }
+    return d;
+}
+
+__device__ __forceinline__ float row_interp(const DustTabs& T, const float* tab, float q, int s) {
+    int j;
+    float w;
+    mc_row_search(T.F + s * MC_NROW, q, j, w);
+    return tab[j] + w * (tab[j + 1] - tab[j]);
+}
+
+__device__ __forceinline__ int reemit_lambda(const DustTabs& T, int nl, Pkt& p, uint32_t k0,
+                                             uint32_t k1, float2 q, int s) {
+    float uq = mc_next(p.rng, k0, k1);
+    float qq = q.x + uq * q.y;
+    int j;
+    float w;
+    mc_row_search(T.F + s * MC_NROW, qq, j, w);
+    int row = j + ((mc_next(p.rng, k0, k1) < w) ? 1 : 0);
+    return mc_cdf_search(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, mc_next(p.rng, k0, k1));
+}
+
+__device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* star_cdf, int nl,
+                                     uint32_t k0, uint32_t k1) {
+    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+    float sn, cs;
+    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+    p.kx = st * cs;
+    p.ky = st * sn;
+    p.kz = mu;
+    p.lam = mc_cdf_search(star_cdf, nl, mc_next(p.rng, k0, k1));
+    p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+    p.x = 0.0; p.y = 0.0; p.z = 0.0;
+    p.dsafe = 0.0;
+    p.ir = -1; p.itv = 0; p.ip = 0;
+    p.last_wall = W_NONE;
+    p.cell_events = 0;
+    p.nevents = 0;
+    p.ncross = 0;
+}
+
+// One transport step: a wall crossing or an interaction.  Returns false when the packet
+// has left the grid or was killed.
+template <int NS>
+__device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) {
+    const McModel& M = P.models[p.m];
+    const double* __restrict__ dp = P.dpool;
+    const int nl = P.nl;
+    const uint32_t k0 = P.key0, k1 = P.key1;
+    int c = -1;
+    float alpha = 0.0f;
+    float rh[NS];
+    const int64_t base = M.cell_off;
+    if (p.ir >= 0) {
+        c = cell_of(M, p);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            rh[s] = __ldg(P.rho + base + (int64_t)s * M.ncell + c);
+            alpha = alpha + rh[s] * T.kext[s * nl + p.lam];
+        }
+    }
+    // Safety distance: an interaction closer than the isotropic distance to the nearest
+    // wall needs no wall solve (the common case in optically thick cells).
+    bool full = true;
+    double se = 0.0;
+    if (alpha > 0.0f) {
+        float sef = p.tau / alpha;
+        if ((double)sef < p.dsafe) { full = false; se = (double)sef; }
+    }
+    int wall = W_NONE;
+    double sw = 0.0;
+    float tcell = 0.0f;
+    bool is_event = true;
+    if (full) {
+        sw = next_wall(M, dp, p, wall);
+        tcell = alpha * (float)sw;
+        is_event = tcell > p.tau;
+        if (is_event) {
+            se = (double)(p.tau / alpha);
+            if (se > sw) se = sw;
+        }
+    }
+    if (is_event) {
+        p.x = p.x + se * (double)p.kx;
+        p.y = p.y + se * (double)p.ky;
+        p.z = p.z + se * (double)p.kz;
+        p.dsafe = full ? 0.0 : p.dsafe - se;
+        p.last_wall = W_NONE;
+        p.cell_events += 1;
+        p.nevents += 1;
+        cnt.events += 1;
+        const bool late = P.late_after > 0 && p.nevents > P.late_after;
+        int64_t* dep = late ? P.Elate : P.E;
+        const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
+        bool did_mrw = false;
+        // MRW is tried after mrw_count_trigger events in one cell, and at every event once
+        // the packet has made more than mrw_eager_after events (it is trapped).
+        if (P.mrw && (p.cell_events >= P.mrw_trigger ||
+                      (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after))) {
+            double R0 = 0.999 * wall_distance(M, dp, p);
+            float R0f = (float)R0;
+            float2 qv[NS];
+            float aR = 0.0f;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                qv[s] = qa[base + (int64_t)s * M.ncell + c];
+                aR = aR + rh[s] * row_interp(T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+            }
+            if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
+                did_mrw = true;
+                float uy = mc_next(p.rng, k0, k1);
+                float f = uy * (float)(MC_NMRW - 1);
+                int i = (int)f;
+                if (i > MC_NMRW - 2) i = MC_NMRW - 2;
+                float w = f - (float)i;
+                float yv = T.mrw[i] + w * (T.mrw[i + 1] - T.mrw[i]);
+                float ell = 3.0f * aR * R0f * R0f * yv;
+                float kp[NS];
+                float aP = 0.0f;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    kp[s] = rh[s] * row_interp(T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                    aP = aP + kp[s];
+                    float units_f = kp[s] * ell * 1048576.0f + 0.5f;
+                    if (units_f > 9.0e18f) units_f = 9.0e18f;
+                    long long units = (long long)units_f;
+                    if (units > 0)
+                        atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
+                                  (unsigned long long)units);
+                }
+                float dx, dy, dz;
+                {
+                    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+                    float sn, cs;
+                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+                    dx = st * cs; dy = st * sn; dz = mu;
+                }
+                p.x = p.x + R0 * (double)dx;
+                p.y = p.y + R0 * (double)dy;
+                p.z = p.z + R0 * (double)dz;
+                {
+                    float mu = sqrtf(mc_next(p.rng, k0, k1));
+                    float sn, cs;
+                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    float kx = dx, ky = dy, kz = dz;
+                    mc_rotate(kx, ky, kz, mu, cs, sn);
+                    p.kx = kx; p.ky = ky; p.kz = kz;
+                }
+                int sp = 0;
+                if (NS > 1) {
+                    float us = mc_next(p.rng, k0, k1) * aP;
+                    float acc = 0.0f;
+                    sp = NS - 1;
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        acc = acc + kp[s];
+                        if (us < acc) { sp = s; break; }
+                    }
+                }
+                float2 qs = qv[0];
+#pragma unroll
+                for (int s = 1; s < NS; ++s)
+                    if (s == sp) qs = qv[s];
+                p.lam = reemit_lambda(T, nl, p, k0, k1, qs, sp);
+                p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+                p.cell_events = 0;
+                cnt.mrw += 1;
+            }
+        }
+        if (!did_mrw) {
+            float ua = mc_next(p.rng, k0, k1);
+            float asca = 0.0f;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + p.lam];
+            if (ua * alpha < asca) {
+                int sp = 0;
+                if (NS > 1) {
+                    float us = mc_next(p.rng, k0, k1) * asca;
+                    float acc = 0.0f;
+                    sp = NS - 1;
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        acc = acc + rh[s] * T.ksca[s * nl + p.lam];
+                        if (us < acc) { sp = s; break; }
+                    }
+                }
+                float g = T.g[sp * nl + p.lam];
+                float umu = mc_next(p.rng, k0, k1);
+                float mu;
+                if (fabsf(g) < 1.0e-4f) {
+                    mu = 2.0f * umu - 1.0f;
+                } else {
+                    float t = (1.0f - g * g) / (1.0f - g + 2.0f * g * umu);
+                    mu = (1.0f + g * g - t * t) / (2.0f * g);
+                    if (mu < -1.0f) mu = -1.0f;
+                    if (mu > 1.0f) mu = 1.0f;
+                }
+                float sn, cs;
+                mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                mc_rotate(p.kx, p.ky, p.kz, mu, cs, sn);
+                cnt.scatter += 1;
+            } else {
+                int sp = 0;
+                if (NS > 1) {
+                    float aabs = 0.0f;
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + p.lam];
+                    float us = mc_next(p.rng, k0, k1) * aabs;
+                    float acc = 0.0f;
+                    sp = NS - 1;
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        acc = acc + rh[s] * T.kabs[s * nl + p.lam];
+                        if (us < acc) { sp = s; break; }
+                    }
+                }
+                int64_t idx = base + (int64_t)sp * M.ncell + c;
+                atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
+                p.lam = reemit_lambda(T, nl, p, k0, k1, qa[idx], sp);
+                {
+                    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+                    float sn, cs;
+                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+                    p.kx = st * cs; p.ky = st * sn; p.kz = mu;
+                }
+                cnt.absorb += 1;
+            }
+            p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+        }
+        if (did_mrw) p.dsafe = 0.0;
+        else if (full) p.dsafe = 0.999999 * wall_distance(M, dp, p);
+        if (late) cnt.late += 1;
+        if (p.nevents >= P.max_inter) {
+            cnt.killed += 1;
+            return false;
+        }
+        if (P.late_after > 0 && p.nevents == P.late_after && P.phase == 0) {
+            if (P.pilot) return false;   // later deposits of pilot packets are discarded
+            unsigned long long slot = atomicAdd(P.park_count, 1ull);
+            if ((long long)slot < P.park_cap) {
+                ParkRec r;
+                r.x = p.x; r.y = p.y; r.z = p.z; r.dsafe = p.dsafe;
+                r.kx = p.kx; r.ky = p.ky; r.kz = p.kz; r.tau = p.tau;
+                r.ir = p.ir; r.itv = p.itv; r.ip = p.ip; r.lam = p.lam;
+                r.last_wall = p.last_wall; r.cell_events = p.cell_events;
+                r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
+                r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag; r.draw = p.rng.draw;
+                r.pad[0] = 0; r.pad[1] = 0;
+                P.park[slot] = r;
+                cnt.parked += 1;
+                return false;
+            }
+        }
+        return true;
+    }
+    p.x = p.x + sw * (double)p.kx;
+    p.y = p.y + sw * (double)p.ky;
+    p.z = p.z + sw * (double)p.kz;
+    p.tau = p.tau - tcell;
+    p.dsafe = 0.0;
+    p.ncross += 1;
+    cnt.crossings += 1;
+    p.cell_events = 0;
+    switch (wall) {
+        case W_ROUT:
+            if (p.ir < 0) { p.ir = 0; locate_angles(M, dp, p); }
+            else p.ir += 1;
+            p.last_wall = W_RIN;
+            if (p.ir >= M.nr) {
+                cnt.escaped += 1;
+                if (P.escape) atomicAdd((unsigned long long*)(P.escape + (int64_t)p.m * nl + p.lam), 1ull);
+                return false;
+            }
+            break;
+        case W_RIN: p.ir -= 1; p.last_wall = W_ROUT; break;
+        case W_TLO: p.itv -= 1; p.last_wall = W_THI; break;
+        case W_THI: p.itv += 1; p.last_wall = W_TLO; break;
+        case W_PLO: p.ip = (p.ip == 0) ? M.np - 1 : p.ip - 1; p.last_wall = W_PHI; break;
+        case W_PHI: p.ip = (p.ip == M.np - 1) ? 0 : p.ip + 1; p.last_wall = W_PLO; break;
+        default: cnt.killed += 1; return false;
+    }
+    if (p.ncross > 100000000) {
+        cnt.killed += 1;
+        return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ long long warp_sum(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
+    extern __shared__ float4 smem4[];
+    float* sm = reinterpret_cast<float*>(smem4);
+    int64_t* s_cum = reinterpret_cast<int64_t*>(sm + ((P.use_smem ? P.dust_floats : 0) + 3) / 4 * 4);
+    __shared__ int s_stop;
+    __shared__ long long s_total;
+    if (threadIdx.x == 0) {
+        s_stop = (*(volatile long long*)(P.stats + ST_STOP) != 0) ? 1 : 0;
+        long long tot = P.total;
+        if (P.phase == 1) {
+            long long c = (long long)*(volatile unsigned long long*)P.park_count;
+            tot = c < P.park_cap ? c : P.park_cap;
+        }
+        s_total = tot;
+        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
+    }
+    const float* tab = P.fpool;
+    if (P.use_smem) {
+        const float4* src = reinterpret_cast<const float4*>(P.fpool);
+        int n4 = (P.dust_floats + 3) / 4;
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) smem4[i] = __ldg(src + i);
+        tab = sm;
+    }
+    for (int i = threadIdx.x; i <= P.nm; i += blockDim.x) s_cum[i] = P.cum[i];
+    __syncthreads();
+    const long long total = s_total;
+    DustTabs T;
+    T.kabs = tab + P.o_kabs; T.ksca = tab + P.o_ksca; T.kext = tab + P.o_kext; T.g = tab + P.o_g;
+    T.F = tab + P.o_F; T.cdf = tab + P.o_cdf; T.kP = tab + P.o_kP; T.kR = tab + P.o_kR;
+    T.mrw = tab + P.o_mrw;
+
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Pkt p;
+    bool active = false;
+    unsigned iter = 0;
+    // Continuations are long by construction: spread them one per warp over the SMs
+    // (packet g -> block g mod grid, then warp, then lane) so that they do not share a
+    // warp's issue slots; the epoch launches use the dynamic warp-aggregated queue.
+    const int wpb = blockDim.x >> 5;
+    const int warp_in_block = threadIdx.x >> 5;
+    long long kstatic = 0;
+    for (;;) {
+        if (s_stop) break;
+        if (P.phase == 1) {
+            if (!active) {
+                long long g = (long long)blockIdx.x +
+                              (long long)gridDim.x * (warp_in_block + (long long)wpb * (lane + 32 * kstatic));
+                if (g < total) {
+                    ++kstatic;
+                    const ParkRec r = P.park[g];
+                    p.x = r.x; p.y = r.y; p.z = r.z; p.dsafe = r.dsafe;
+                    p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
+                    p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
+                    p.last_wall = r.last_wall; p.cell_events = r.cell_events;
+                    p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
+                    p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag; p.rng.draw = r.draw;
+                    if (p.rng.draw & 3u) {
+                        uint4 o = philox4x32_10(make_uint4(p.rng.draw >> 2, p.rng.pid, p.rng.model, p.rng.tag),
+                                                P.key0, P.key1);
+                        p.rng.b0 = o.x; p.rng.b1 = o.y; p.rng.b2 = o.z; p.rng.b3 = o.w;
+                    }
+                    active = true;
+                }
+            }
+        } else {
+        unsigned need = __ballot_sync(0xffffffffu, !active);
+        if (need) {
+            int n = __popc(need);
+            unsigned long long basev = 0;
+            if (lane == 0) basev = atomicAdd(P.queue, (unsigned long long)n);
+            basev = __shfl_sync(0xffffffffu, basev, 0);
+            if (!active) {
+                long long g = (long long)basev + __popc(need & lt_mask);
+                if (g < total) {
+                    int lo = 0, hi = P.nm;
+                    while (hi - lo > 1) {
+                        int mid = (lo + hi) >> 1;
+                        if (s_cum[mid] <= g) lo = mid; else hi = mid;
+                    }
+                    const McModel& M = P.models[lo];
+                    p.m = lo;
+                    p.epoch = P.epoch;
+                    p.rng.pid = (uint32_t)(M.bnd[P.epoch] + (g - s_cum[lo]));
+                    p.rng.model = (uint32_t)M.model_id;
+                    p.rng.tag = P.tag;
+                    p.rng.draw = 0;
+                    emit(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
+                    active = true;
+                }
+            }
+        }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            active = mc_step<NS>(p, P, T, cnt);
+            if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
+        }
+        if (((++iter) & 4095u) == 0u) {
+            int stop = 0;
+            if (lane == 0) {
+                if (*(volatile long long*)(P.stats + ST_STOP) != 0) stop = 1;
+                if (P.abort_flag && *P.abort_flag != 0) {
+                    atomicCAS((unsigned long long*)(P.stats + ST_STATUS), 0ull, (unsigned long long)PDGPU_ABORTED);
+                    stop = 1;
+                }
+                if (P.deadline_ns > 0) {
+                    long long t0 = P.stats[ST_T0];
+                    if ((long long)globaltimer() - t0 > P.deadline_ns) {
+                        atomicCAS((unsigned long long*)(P.stats + ST_STATUS), 0ull, (unsigned long long)PDGPU_TIMEOUT);
+                        stop = 1;
+                    }
+                }
+                if (stop) atomicExch((unsigned long long*)(P.stats + ST_STOP), 1ull);
+            }
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            if (stop) break;
+        }
+    }
+    if (P.count_stats) {
+        long long v[9] = {cnt.killed, cnt.escaped, cnt.crossings, cnt.events, cnt.absorb,
+                          cnt.scatter, cnt.mrw, cnt.late, cnt.parked};
+        const int slot[9] = {ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
+                             ST_MRW, ST_LATE, ST_PARKED};
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            long long s = warp_sum(v[i]);
+            if (lane == 0 && s) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)s);
+        }
+    }
+    int mx = cnt.maxev;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    long long pk = warp_sum(cnt.parked);
+    if (lane == 0) {
+        int64_t* L = P.stats + MC_LSTAT + 4 * P.lslot;
+        atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
+        atomicMax((unsigned long long*)(L + 2), (unsigned long long)mx);
+        if (pk) atomicAdd((unsigned long long*)(L + 3), (unsigned long long)pk);
+    }
+}
+
+// Per-epoch cell preparation: (q_lo, q_span) in erg/s/g from the absorbed energy.
+struct PrepParams {
+    const McModel* models;
+    const double* dpool;
+    const float* rho;
+    const int64_t* src;       // energy the span is computed from
+    float2* q;
+    int64_t total;            // total cells over models and species
+    int32_t nm, ns;
+    int32_t first;            // 1: first epoch (q_lo = 0, q_span = src/m)
+    int32_t epoch;            // epoch k >= 1 (ratio b_{k+1}/b_k)
+};
+
+__device__ __forceinline__ int model_of_cell(const McModel* models, int nm, int ns, int64_t i) {
+    int lo = 0, hi = nm;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (models[mid].cell_off <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ double cell_mass(const McModel& M, const double* dp, float rho, int c) {
+    int ip = c % M.np;
+    int t = c / M.np;
+    int it = t % M.nt;
+    int ir = t / M.nt;
+    double V = dp[M.off_vr + ir] * dp[M.off_vt + it] * dp[M.off_vp + ip];
+    return (double)rho * V;
+}
+
+__global__ void mc_prep_kernel(PrepParams P) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int m = model_of_cell(P.models, P.nm, P.ns, i);
+        const McModel& M = P.models[m];
+        int c = (int)((i - M.cell_off) % M.ncell);
+        double mass = cell_mass(M, P.dpool, P.rho[i], c);
+        float2 out = make_float2(0.0f, 0.0f);
+        if (mass > 0.0) {
+            double e = (double)P.src[i];
+            if (P.first) {
+                out.y = (float)(e * M.q_unit / mass);
+            } else {
+                double R = (double)M.bnd[P.epoch + 1] / (double)M.bnd[P.epoch];
+                out.x = (float)(e * M.q_unit / mass);
+                out.y = (float)(e * M.q_unit * (R - 1.0) / mass);
+            }
+        }
+        P.q[i] = out;
+    }
+}
+
+struct TempParams {
+    const McModel* models;
+    const double* dpool;
+    const float* rho;
+    const int64_t* E;
+    const int64_t* Elate;
+    double* T;
+    int64_t total;
+    int32_t nm, ns;
+    int32_t off_tinv, off_finv;   // dpool offsets
+};
+
+__global__ void mc_temperature_kernel(TempParams P) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int m = model_of_cell(P.models, P.nm, P.ns, i);
+        const McModel& M = P.models[m];
+        int64_t rel = i - M.cell_off;
+        int s = (int)(rel / M.ncell);
+        int c = (int)(rel % M.ncell);
+        double mass = cell_mass(M, P.dpool, P.rho[i], c);
+        int64_t E = P.E[i] + P.Elate[i];
+        double T = 0.0;
+        if (E > 0 && mass > 0.0) {
+            const double* F = P.dpool + P.off_finv + (size_t)s * MC_NINV;
+            const double* TV = P.dpool + P.off_tinv;
+            double q = (double)E * M.q_unit / mass;
+            if (q <= F[0]) {
+                T = TV[0] * sqrt(sqrt(q / F[0]));
+            } else if (q >= F[MC_NINV - 1]) {
+                T = TV[MC_NINV - 1];
+            } else {
+                int lo = 0, hi = MC_NINV - 1;
+                while (hi - lo > 1) {
+                    int mid = lo + (hi - lo) / 2;
+                    if (F[mid] <= q) lo = mid; else hi = mid;
+                }
+                T = TV[lo] + (TV[lo + 1] - TV[lo]) * ((q - F[lo]) / (F[lo + 1] - F[lo]));
+            }
+        }
+        P.T[i] = T;
+    }
+}
+
+__global__ void mc_start_kernel(int64_t* stats) {
+    stats[ST_T0] = (int64_t)globaltimer();
+    for (int l = 0; l < MC_MAX_LAUNCH; ++l) stats[MC_LSTAT + 4 * l] = 0x7fffffffffffffffLL;
+}
+
+__global__ void mc_finish_kernel(int64_t* stats, int64_t packets) {
+    stats[ST_PACKETS] = packets;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// Host side: tables, geometry, schedule.  The same formulas as the CPU oracle, evaluated in
+// the same order, so both consume identical tables.
+// ---------------------------------------------------------------------------------------
+struct pdgpu_mc_plan {
+    int nm, ns, nl, K, npilot;
+    pdgpu_mc_options opt;
+    std::vector<float> fpool;       // dust tables first (dust_floats), then star CDFs
+    std::vector<double> dpool;      // walls per model, Tinv, Finv
+    std::vector<McModel> models;
+    std::vector<int64_t> cum;       // [K][nm+1]
+    int dust_floats;
+    int o_kabs, o_ksca, o_kext, o_g, o_F, o_cdf, o_kP, o_kR, o_mrw;
+    int off_tinv, off_finv;
+    int64_t total_cells, total_nphot;
+    // workspace layout
+    size_t ws_fpool, ws_dpool, ws_models, ws_cum, ws_E, ws_D, ws_q, ws_escape, ws_stats,
+        ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_parkcnt;
+    int64_t park_cap;
+    int nqueue;
+    int device, nsm, block, grid;
+    bool smem_tables;
+    size_t smem_bytes;
+    void* uploaded_ws;
+    cudaEvent_t ev[2 * MC_MAX_LAUNCH];   // launch timing (time_launches)
+    bool ev_ready;
+    int ev_used;
+};
+
+namespace {
+
+double planck_nu(double nu, double T) {
+    double x = MC_H_PLANCK * nu / (MC_K_BOLTZ * T);
+    if (x > 700.0) return 0.0;
+    double pre = 2.0 * MC_H_PLANCK * nu * nu * nu / (MC_C_LIGHT * MC_C_LIGHT);
+    return pre / expm1(x);
+}
+
+double dplanck_dT(double nu, double T) {
+    double x = MC_H_PLANCK * nu / (MC_K_BOLTZ * T);
+    if (x > 700.0) return 0.0;
+    double em1 = expm1(x);
+    double pre = 2.0 * MC_H_PLANCK * nu * nu * nu / (MC_C_LIGHT * MC_C_LIGHT);
+    double bb = pre / em1;
+    return bb * (x * exp(x) / em1) / T;
+}
+
+double mrw_survival(double y) {
+    if (y < 0.005) return 1.0;
+    double s = 0.0;
+    for (int n = 1; n < 100000; ++n) {
+        double a = (double)n * (double)n * MC_PI * MC_PI * y;
+        if (a > 80.0) break;
+        double t = exp(-a);
+        s += (n & 1) ? t : -t;
+    }
+    return 2.0 * s;
+}
+
+const std::vector<float>& mrw_table() {
+    static std::vector<float> tab;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        tab.resize(MC_NMRW);
+        for (int i = 0; i < MC_NMRW; ++i) {
+            double xi = (double)i / (double)(MC_NMRW - 1);
+            if (i == MC_NMRW - 1) { tab[i] = 0.0f; continue; }
+            if (i == 0) xi = 1.0e-7;
+            double lo = 0.0, hi = 10.0;
+            for (int it = 0; it < 100; ++it) {
+                double mid = 0.5 * (lo + hi);
+                if (mrw_survival(mid) > xi) lo = mid; else hi = mid;
+            }
+            tab[i] = (float)(0.5 * (lo + hi));
+        }
+    });
+    return tab;
+}
+
+pdgpu_status build_dust(pdgpu_mc_plan* P, const pdgpu_dust_desc* d, std::vector<double>& nu,
+                        std::vector<double>& dnu) {
+    int nl = d->nlam, ns = d->nspec;
+    nu.resize(nl);
+    dnu.resize(nl);
+    for (int l = 0; l < nl; ++l) nu[l] = MC_C_LIGHT / (d->lam_um[l] * 1.0e-4);
+    for (int l = 0; l < nl; ++l) {
+        if (l == 0) dnu[l] = 0.5 * fabs(nu[0] - nu[1]);
+        else if (l == nl - 1) dnu[l] = 0.5 * fabs(nu[nl - 2] - nu[nl - 1]);
+        else dnu[l] = 0.5 * fabs(nu[l - 1] - nu[l + 1]);
+    }
+    std::vector<float>& f = P->fpool;
+    auto take = [&](size_t n) {
+        int off = (int)f.size();
+        f.resize(f.size() + n, 0.0f);
+        return off;
+    };
+    P->o_kabs = take((size_t)ns * nl);
+    P->o_ksca = take((size_t)ns * nl);
+    P->o_kext = take((size_t)ns * nl);
+    P->o_g = take((size_t)ns * nl);
+    for (int i = 0; i < ns * nl; ++i) {
+        f[P->o_kabs + i] = (float)d->kabs[i];
+        f[P->o_ksca + i] = (float)d->ksca[i];
+        f[P->o_kext + i] = f[P->o_kabs + i] + f[P->o_ksca + i];
+        f[P->o_g + i] = d->g ? (float)d->g[i] : 0.0f;
+    }
+    P->o_F = take((size_t)ns * MC_NROW);
+    P->o_cdf = take((size_t)ns * MC_NROW * nl);
+    P->o_kP = take((size_t)ns * MC_NROW);
+    P->o_kR = take((size_t)ns * MC_NROW);
+    std::vector<double> cumv(nl);
+    for (int s = 0; s < ns; ++s) {
+        const double* ka = d->kabs + (size_t)s * nl;
+        const double* ks = d->ksca + (size_t)s * nl;
+        for (int j = 0; j < MC_NROW; ++j) {
+            double T = MC_TROW_LO * pow(MC_TROW_HI / MC_TROW_LO, (double)j / (double)(MC_NROW - 1));
+            double sumF = 0.0, sumB = 0.0, sumD = 0.0, sumDk = 0.0, c = 0.0;
+            for (int l = 0; l < nl; ++l) {
+                double B = planck_nu(nu[l], T);
+                double dB = dplanck_dT(nu[l], T);
+                sumF += ka[l] * B * dnu[l];
+                sumB += B * dnu[l];
+                sumD += dB * dnu[l];
+                double ke = ka[l] + ks[l];
+                if (ke > 0.0) sumDk += dB / ke * dnu[l];
+                c += ka[l] * dB * dnu[l];
+                cumv[l] = c;
+            }
+            double Fj = 4.0 * MC_PI * sumF;
+            f[P->o_F + s * MC_NROW + j] = (float)Fj;
+            float* row = &f[P->o_cdf + ((size_t)s * MC_NROW + j) * nl];
+            for (int l = 0; l < nl; ++l)
+                row[l] = (c > 0.0) ? (float)(cumv[l] / c) : (float)((l + 1.0) / nl);
+            row[nl - 1] = 1.0f;
+            f[P->o_kP + s * MC_NROW + j] = (float)(sumB > 0.0 ? sumF / sumB : 0.0);
+            f[P->o_kR + s * MC_NROW + j] = (float)(sumDk > 0.0 ? sumD / sumDk : 0.0);
+        }
+    }
+    P->o_mrw = take(MC_NMRW);
+    const std::vector<float>& mt = mrw_table();
+    for (int i = 0; i < MC_NMRW; ++i) f[P->o_mrw + i] = mt[i];
+    P->dust_floats = (int)f.size();
+    // pad to 16 bytes so the stellar CDFs start aligned
+    while (f.size() % 4) f.push_back(0.0f);
+    return PDGPU_OK;
+}
+
+int pick_device_props(int& nsm) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    return dev;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t pdgpu_abi_version(void) { return PDGPU_ABI_VERSION; }
+
+const char* pdgpu_status_string(pdgpu_status s) {
+    switch (s) {
+        case PDGPU_OK: return "ok";
+        case PDGPU_INVALID_ARG: return "invalid argument";
+        case PDGPU_TIMEOUT: return "time limit reached";
+        case PDGPU_ABORTED: return "aborted by the host";
+        case PDGPU_PACKET_CAP: return "packets hit the interaction cap";
+        case PDGPU_OVERFLOW: return "fixed-point overflow";
+        case PDGPU_CUDA_ERROR: return "CUDA error";
+        case PDGPU_NO_DEVICE: return "no usable CUDA device";
+        case PDGPU_WORKSPACE: return "workspace missing, too small or not uploaded";
+        default: return "unknown status";
+    }
+}
+
+pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* models,
+                                  const pdgpu_dust_desc* dust, const pdgpu_mc_options* options,
+                                  pdgpu_mc_plan** out) {
+    if (!out) return PDGPU_INVALID_ARG;
+    *out = nullptr;
+    if (nmodels < 1 || !models || !dust || !options) return PDGPU_INVALID_ARG;
+    if (dust->nlam < 2 || dust->nspec < 1 || dust->nspec > MC_MAX_SPEC || !dust->lam_um ||
+        !dust->kabs || !dust->ksca)
+        return PDGPU_INVALID_ARG;
+    for (int l = 1; l < dust->nlam; ++l)
+        if (!(dust->lam_um[l] > dust->lam_um[l - 1])) return PDGPU_INVALID_ARG;
+    for (int i = 0; i < dust->nspec * dust->nlam; ++i)
+        if (!(dust->kabs[i] >= 0.0) || !(dust->ksca[i] >= 0.0) || !std::isfinite(dust->kabs[i]) ||
+            !std::isfinite(dust->ksca[i]))
+            return PDGPU_INVALID_ARG;
+    pdgpu_mc_plan* P = new (std::nothrow) pdgpu_mc_plan();
+    if (!P) return PDGPU_INVALID_ARG;
+    P->nm = nmodels;
+    P->ns = dust->nspec;
+    P->nl = dust->nlam;
+    P->opt = *options;
+    P->K = options->nepoch < 1 ? 1 : std::min(options->nepoch, MC_MAX_EPOCH);
+    P->npilot = std::max(0, options->npilot);
+    P->K = std::min(P->K, MC_MAX_LAUNCH - 2);
+    P->npilot = std::min(P->npilot, MC_MAX_LAUNCH - 1 - P->K);
+    // fewer epochs when a model has too few packets for the first epoch to be non-empty
+    for (int m = 0; m < nmodels; ++m)
+        while (P->K > 1 && (models[m].nphot >> (P->K - 1)) == 0) P->K--;
+    std::vector<double> nu, dnu;
+    build_dust(P, dust, nu, dnu);
+    const int ns = P->ns, nl = P->nl;
+    // temperature inversion tables
+    P->off_tinv = (int)P->dpool.size();
+    for (int j = 0; j < MC_NINV; ++j)
+        P->dpool.push_back(MC_TINV_LO * pow(MC_TINV_HI / MC_TINV_LO, (double)j / (double)(MC_NINV - 1)));
+    P->off_finv = (int)P->dpool.size();
+    for (int s = 0; s < ns; ++s) {
+        const double* ka = dust->kabs + (size_t)s * nl;
+        for (int j = 0; j < MC_NINV; ++j) {
+            double sumF = 0.0;
+            for (int l = 0; l < nl; ++l) sumF += ka[l] * planck_nu(nu[l], P->dpool[P->off_tinv + j]) * dnu[l];
+            P->dpool.push_back(4.0 * MC_PI * sumF);
+        }
+    }
+    int64_t cell_off = 0;
+    P->total_nphot = 0;
+    for (int m = 0; m < nmodels; ++m) {
+        const pdgpu_model_desc& d = models[m];
+        McModel M;
+        memset(&M, 0, sizeof(M));
+        if (d.nr < 1 || d.ntheta < 1 || d.nphi < 1 || !d.r_edges_cm || !d.theta_edges ||
+            !d.phi_edges || d.nstar < 1 || !d.star_radius_cm || !d.star_temperature ||
+            d.nphot < 1 || d.nphot > 4000000000LL) {
+            delete P;
+            return PDGPU_INVALID_ARG;
+        }
+        if (!(d.r_edges_cm[0] > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
+        for (int i = 1; i <= d.nr; ++i)
+            if (!(d.r_edges_cm[i] > d.r_edges_cm[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
+        for (int i = 1; i <= d.ntheta; ++i)
+            if (!(d.theta_edges[i] > d.theta_edges[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
+        for (int i = 1; i <= d.nphi; ++i)
+            if (!(d.phi_edges[i] > d.phi_edges[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
+        double thmax = d.theta_edges[d.ntheta];
+        if (fabs(d.theta_edges[0]) > 1e-12) { delete P; return PDGPU_INVALID_ARG; }
+        if (fabs(thmax - MC_PI) < 1e-9) M.mirror = 0;
+        else if (fabs(thmax - 0.5 * MC_PI) < 1e-9) M.mirror = 1;
+        else { delete P; return PDGPU_INVALID_ARG; }
+        if (d.nphi > 1 && (fabs(d.phi_edges[0]) > 1e-12 || fabs(d.phi_edges[d.nphi] - 2.0 * MC_PI) > 1e-9)) {
+            delete P;
+            return PDGPU_INVALID_ARG;
+        }
+        M.nr = d.nr; M.nt = d.ntheta; M.np = d.nphi;
+        M.ntv = M.mirror ? 2 * d.ntheta : d.ntheta;
+        M.ncell = d.nr * d.ntheta * d.nphi;
+        M.cell_off = cell_off;
+        M.model_id = m;
+        M.nphot = d.nphot;
+        std::vector<double>& dp = P->dpool;
+        M.off_r = (int)dp.size();
+        for (int i = 0; i <= d.nr; ++i) dp.push_back(d.r_edges_cm[i]);
+        M.off_mu = (int)dp.size();
+        dp.resize(dp.size() + M.ntv + 1);
+        M.off_sn = (int)dp.size();
+        dp.resize(dp.size() + M.ntv + 1);
+        int nt = d.ntheta;
+        for (int j = 0; j <= nt; ++j) {
+            double th = d.theta_edges[j];
+            double mv = cos(th), sv = sin(th);
+            if (fabs(th - 0.5 * MC_PI) < 1e-12) { mv = 0.0; sv = 1.0; }
+            if (j == 0) { mv = 1.0; sv = 0.0; }
+            if (!M.mirror && j == nt) { mv = -1.0; sv = 0.0; }
+            dp[M.off_mu + j] = mv;
+            dp[M.off_sn + j] = sv;
+        }
+        if (M.mirror)
+            for (int j = 0; j < nt; ++j) {
+                dp[M.off_mu + 2 * nt - j] = -dp[M.off_mu + j];
+                dp[M.off_sn + 2 * nt - j] = dp[M.off_sn + j];
+            }
+        M.off_cph = (int)dp.size();
+        for (int k = 0; k <= d.nphi; ++k) dp.push_back(cos(d.phi_edges[k]));
+        M.off_sph = (int)dp.size();
+        for (int k = 0; k <= d.nphi; ++k) dp.push_back(sin(d.phi_edges[k]));
+        M.off_vr = (int)dp.size();
+        for (int i = 0; i < d.nr; ++i) {
+            double r0 = d.r_edges_cm[i], r1 = d.r_edges_cm[i + 1];
+            dp.push_back((r1 * r1 * r1 - r0 * r0 * r0) / 3.0);
+        }
+        M.off_vt = (int)dp.size();
+        for (int j = 0; j < nt; ++j) {
+            double v = dp[M.off_mu + j] - dp[M.off_mu + j + 1];
+            dp.push_back(M.mirror ? 2.0 * v : v);
+        }
+        M.off_vp = (int)dp.size();
+        for (int k = 0; k < d.nphi; ++k) dp.push_back(d.phi_edges[k + 1] - d.phi_edges[k]);
+        for (int k = 0; k <= d.nphi; ++k) dp.push_back(d.phi_edges[k]);  // edges after widths
+        // stellar spectrum
+        std::vector<double> Lnu(nl, 0.0);
+        for (int s = 0; s < d.nstar; ++s) {
+            double R = d.star_radius_cm[s];
+            if (!(R > 0.0) || !(d.star_temperature[s] > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
+            for (int l = 0; l < nl; ++l)
+                Lnu[l] += 4.0 * MC_PI * R * R * MC_PI * planck_nu(nu[l], d.star_temperature[s]) * dnu[l];
+        }
+        double L = 0.0;
+        for (int l = 0; l < nl; ++l) L += Lnu[l];
+        if (!(L > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
+        M.lum = L;
+        M.off_star = (int)P->fpool.size();
+        double cum = 0.0;
+        for (int l = 0; l < nl; ++l) {
+            cum += Lnu[l];
+            P->fpool.push_back((float)(cum / L));
+        }
+        P->fpool[M.off_star + nl - 1] = 1.0f;
+        while (P->fpool.size() % 4) P->fpool.push_back(0.0f);
+        double eps = L / (double)d.nphot;
+        M.q_unit = eps / (double)((int64_t)1 << MC_EUNIT_SHIFT);
+        // epochs: b_k = N >> (K - k) (K shared by all models, see below)
+        const int K = P->K;
+        for (int k = 0; k <= MC_MAX_EPOCH; ++k) M.bnd[k] = d.nphot;
+        M.bnd[0] = 0;
+        for (int k = 1; k <= K; ++k) M.bnd[k] = d.nphot >> (K - k);
+        P->models.push_back(M);
+        cell_off += (int64_t)ns * M.ncell;
+        P->total_nphot += d.nphot;
+    }
+    P->total_cells = cell_off;
+    // per-epoch prefix sums of packet counts over models
+    P->cum.assign((size_t)P->K * (nmodels + 1), 0);
+    for (int k = 0; k < P->K; ++k) {
+        int64_t acc = 0;
+        for (int m = 0; m < nmodels; ++m) {
+            P->cum[(size_t)k * (nmodels + 1) + m] = acc;
+            acc += P->models[m].bnd[k + 1] - P->models[m].bnd[k];
+        }
+        P->cum[(size_t)k * (nmodels + 1) + nmodels] = acc;
+    }
+    // device properties and launch shape
+    int nsm = 0;
+    P->device = pick_device_props(nsm);
+    P->nsm = nsm > 0 ? nsm : 1;
+    P->block = options->block_threads > 0 ? options->block_threads : 256;
+    if (P->block > 256) P->block = 256;
+    size_t dust_bytes = ((size_t)P->dust_floats + 3) / 4 * 16;
+    size_t cum_bytes = (size_t)(nmodels + 1) * sizeof(int64_t);
+    int smem_max = 0;
+    if (P->device >= 0)
+        cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->device);
+    P->smem_tables = (dust_bytes + cum_bytes + 64) <= (size_t)smem_max;
+    P->smem_bytes = (P->smem_tables ? dust_bytes : 0) + cum_bytes + 16;
+    // workspace layout
+    size_t o = 0;
+    auto place = [&](size_t bytes) {
+        o = (o + 255) / 256 * 256;
+        size_t at = o;
+        o += bytes;
+        return at;
+    };
+    P->ws_fpool = place(P->fpool.size() * sizeof(float));
+    P->ws_dpool = place(P->dpool.size() * sizeof(double));
+    P->ws_models = place(P->models.size() * sizeof(McModel));
+    P->ws_cum = place(P->cum.size() * sizeof(int64_t));
+    P->tables_bytes = (o + 255) / 256 * 256;
+    P->ws_E = place((size_t)P->total_cells * sizeof(int64_t));
+    P->ws_D = place((size_t)P->total_cells * sizeof(int64_t));
+    P->ws_q = place((size_t)P->K * P->total_cells * sizeof(float2));
+    P->ws_Elate = place((size_t)P->total_cells * sizeof(int64_t));
+    P->park_cap = std::max<int64_t>(8192, P->total_nphot / 128);
+    P->ws_park = place((size_t)P->park_cap * sizeof(ParkRec));
+    P->ws_parkcnt = place(sizeof(unsigned long long));
+    P->ws_escape = place((size_t)nmodels * nl * sizeof(int64_t));
+    P->ws_stats = place(MC_NSTAT * sizeof(int64_t));
+    P->nqueue = P->K + P->npilot + 1;
+    P->ws_queue = place((size_t)P->nqueue * sizeof(unsigned long long));
+    P->ws_total = (o + 255) / 256 * 256;
+    P->uploaded_ws = nullptr;
+    P->ev_ready = false;
+    P->ev_used = 0;
+    if (options->time_launches && P->device >= 0) {
+        P->ev_ready = true;
+        for (int i = 0; i < 2 * MC_MAX_LAUNCH; ++i)
+            if (cudaEventCreate(&P->ev[i]) != cudaSuccess) P->ev_ready = false;
+    }
+    *out = P;
+    return PDGPU_OK;
+}
+
+void pdgpu_mc_plan_destroy(pdgpu_mc_plan* plan) {
+    if (!plan) return;
+    if (plan->ev_ready)
+        for (int i = 0; i < 2 * MC_MAX_LAUNCH; ++i) cudaEventDestroy(plan->ev[i]);
+    delete plan;
+}
+
+int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* P, float* ms, int32_t capacity) {
+    if (!P || !ms || !P->ev_ready) return 0;
+    int n = std::min(P->ev_used, (int)capacity);
+    for (int i = 0; i < n; ++i) {
+        float t = 0.0f;
+        if (cudaEventSynchronize(P->ev[2 * i + 1]) != cudaSuccess ||
+            cudaEventElapsedTime(&t, P->ev[2 * i], P->ev[2 * i + 1]) != cudaSuccess)
+            t = -1.0f;
+        ms[i] = t;
+    }
+    return n;
+}
+
+pdgpu_status pdgpu_mc_plan_layout(const pdgpu_mc_plan* P, pdgpu_mc_layout* L) {
+    if (!P || !L) return PDGPU_INVALID_ARG;
+    L->tables_bytes = P->tables_bytes;
+    L->energy_offset = P->ws_E;
+    L->late_offset = P->ws_Elate;
+    L->escape_offset = P->ws_escape;
+    L->stats_offset = P->ws_stats;
+    L->total_bytes = P->ws_total;
+    L->total_cells = P->total_cells;
+    L->nmodels = P->nm;
+    L->nspec = P->ns;
+    L->nlam = P->nl;
+    L->smem_tables = P->smem_tables ? 1 : 0;
+    return PDGPU_OK;
+}
+
+pdgpu_status pdgpu_mc_plan_upload(pdgpu_mc_plan* P, void* ws, size_t bytes, void* stream) {
+    if (!P) return PDGPU_INVALID_ARG;
+    if (!ws || bytes < P->ws_total) return PDGPU_WORKSPACE;
+    if (P->device < 0) return PDGPU_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char* w = (char*)ws;
+    if (cudaMemcpyAsync(w + P->ws_fpool, P->fpool.data(), P->fpool.size() * sizeof(float),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(w + P->ws_dpool, P->dpool.data(), P->dpool.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(w + P->ws_models, P->models.data(), P->models.size() * sizeof(McModel),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(w + P->ws_cum, P->cum.data(), P->cum.size() * sizeof(int64_t),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    // pageable sources: make sure the copies finished before the host vectors can change
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PDGPU_CUDA_ERROR;
+    P->uploaded_ws = ws;
+    return PDGPU_OK;
+}
+
+// phase 0: epoch launch over the epoch's packets; phase 1: continuation of parked packets
+static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho, int64_t* target,
+                                     int epoch, uint32_t tag, int lslot, bool final_pass,
+                                     int phase, cudaStream_t st) {
+    McParams prm;
+    memset(&prm, 0, sizeof(prm));
+    prm.fpool = (const float*)(w + P->ws_fpool);
+    prm.dpool = (const double*)(w + P->ws_dpool);
+    prm.models = (const McModel*)(w + P->ws_models);
+    prm.cum = (const int64_t*)(w + P->ws_cum) + (size_t)epoch * (P->nm + 1);
+    prm.rho = rho;
+    prm.E = target;
+    prm.Elate = final_pass ? (int64_t*)(w + P->ws_Elate) : target;
+    prm.q = (const float2*)(w + P->ws_q);
+    prm.qstride = P->total_cells;
+    prm.late_after = P->opt.late_after > 0 ? P->opt.late_after : 0;
+    prm.park = (ParkRec*)(w + P->ws_park);
+    prm.park_count = (unsigned long long*)(w + P->ws_parkcnt);
+    prm.park_cap = P->park_cap;
+    prm.pilot = final_pass ? 0 : 1;
+    prm.phase = phase;
+    prm.lslot = lslot;
+    prm.escape = final_pass ? (int64_t*)(w + P->ws_escape) : nullptr;
+    prm.stats = (int64_t*)(w + P->ws_stats);
+    prm.queue = (unsigned long long*)(w + P->ws_queue) + lslot;
+    prm.abort_flag = P->opt.abort_flag;
+    prm.deadline_ns = P->opt.deadline_ns;
+    prm.total = phase == 0 ? P->cum[(size_t)epoch * (P->nm + 1) + P->nm] : P->park_cap;
+    prm.nm = P->nm;
+    prm.ns = P->ns;
+    prm.nl = P->nl;
+    prm.epoch = epoch;
+    prm.tag = tag;
+    prm.key0 = (uint32_t)(P->opt.seed & 0xffffffffu);
+    prm.key1 = (uint32_t)(P->opt.seed >> 32);
+    prm.mrw = P->opt.mrw;
+    prm.mrw_trigger = P->opt.mrw_count_trigger;
+    prm.mrw_eager_after = (int32_t)std::min<int64_t>(std::max<int64_t>(P->opt.mrw_eager_after, 0),
+                                                     2000000000LL);
+    prm.mrw_gamma = P->opt.mrw_gamma;
+    prm.mrw_tauthres = P->opt.mrw_tauthres;
+    int64_t mi = P->opt.max_interactions <= 0 ? 2000000000LL : P->opt.max_interactions;
+    prm.max_inter = (int32_t)std::min<int64_t>(mi, 2000000000LL);
+    prm.dust_floats = P->dust_floats;
+    prm.use_smem = P->smem_tables ? 1 : 0;
+    prm.o_kabs = P->o_kabs; prm.o_ksca = P->o_ksca; prm.o_kext = P->o_kext; prm.o_g = P->o_g;
+    prm.o_F = P->o_F; prm.o_cdf = P->o_cdf; prm.o_kP = P->o_kP; prm.o_kR = P->o_kR;
+    prm.o_mrw = P->o_mrw;
+    prm.count_stats = final_pass ? 1 : 0;
+    if (prm.total <= 0) return PDGPU_OK;
+    void (*kern)(McParams) = nullptr;
+    switch (P->ns) {
+        case 1: kern = mc_transport_kernel<1>; break;
+        case 2: kern = mc_transport_kernel<2>; break;
+        case 3: kern = mc_transport_kernel<3>; break;
+        default: kern = mc_transport_kernel<4>; break;
+    }
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem_bytes) !=
+        cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P->block, P->smem_bytes) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return PDGPU_CUDA_ERROR;
+    if (P->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)P->opt.blocks_per_sm);
+    int64_t want = (prm.total + P->block - 1) / P->block;
+    int grid = (int)std::min<int64_t>((int64_t)per_sm * P->nsm, std::max<int64_t>(want, 1));
+    if (phase == 1) grid = per_sm * P->nsm;  // parked count is only known on the device
+    P->grid = grid;
+    if (P->opt.time_launches && P->ev_ready) cudaEventRecord(P->ev[2 * lslot], st);
+    kern<<<grid, P->block, P->smem_bytes, st>>>(prm);
+    if (P->opt.time_launches && P->ev_ready) {
+        cudaEventRecord(P->ev[2 * lslot + 1], st);
+        P->ev_used = std::max(P->ev_used, lslot + 1);
+    }
+    return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
+}
+
+static pdgpu_status launch_prep(pdgpu_mc_plan* P, char* w, const float* rho, const int64_t* src,
+                                int first, int epoch, cudaStream_t st) {
+    PrepParams q;
+    q.models = (const McModel*)(w + P->ws_models);
+    q.dpool = (const double*)(w + P->ws_dpool);
+    q.rho = rho;
+    q.src = src;
+    q.q = (float2*)(w + P->ws_q) + (size_t)epoch * P->total_cells;
+    q.total = P->total_cells;
+    q.nm = P->nm;
+    q.ns = P->ns;
+    q.first = first;
+    q.epoch = epoch;
+    int grid = (int)std::min<int64_t>((P->total_cells + 255) / 256, (int64_t)P->nsm * 8);
+    mc_prep_kernel<<<std::max(grid, 1), 256, 0, st>>>(q);
+    return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
+}
+
+pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* P, const float* rho, double* temperature, void* ws,
+                               size_t bytes, void* stream) {
+    if (!P || !rho || !temperature) return PDGPU_INVALID_ARG;
+    if (!ws || bytes < P->ws_total || P->uploaded_ws != ws) return PDGPU_WORKSPACE;
+    if (P->device < 0) return PDGPU_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char* w = (char*)ws;
+    int64_t* E = (int64_t*)(w + P->ws_E);
+    int64_t* D = (int64_t*)(w + P->ws_D);
+    int64_t* EL = (int64_t*)(w + P->ws_Elate);
+    size_t cells_bytes = (size_t)P->total_cells * sizeof(int64_t);
+    if (cudaMemsetAsync(E, 0, cells_bytes, st) != cudaSuccess ||
+        cudaMemsetAsync(D, 0, cells_bytes, st) != cudaSuccess ||
+        cudaMemsetAsync(EL, 0, cells_bytes, st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_parkcnt, 0, sizeof(unsigned long long), st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_escape, 0, (size_t)P->nm * P->nl * sizeof(int64_t), st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_stats, 0, MC_NSTAT * sizeof(int64_t), st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_queue, 0, (size_t)P->nqueue * sizeof(unsigned long long), st) !=
+            cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    mc_start_kernel<<<1, 1, 0, st>>>((int64_t*)(w + P->ws_stats));
+    pdgpu_status rc;
+    int lslot = 0;
+    P->ev_used = 0;
+    // first epoch: pilot passes write D (and stop at late_after), the real pass writes E
+    for (int pass = P->npilot; pass >= 0; --pass) {
+        if ((rc = launch_prep(P, w, rho, D, 1, 0, st)) != PDGPU_OK) return rc;
+        if (pass > 0) {
+            if (cudaMemsetAsync(D, 0, cells_bytes, st) != cudaSuccess) return PDGPU_CUDA_ERROR;
+            rc = launch_transport(P, w, rho, D, 0, (uint32_t)pass, lslot++, false, 0, st);
+        } else {
+            rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 0, st);
+        }
+        if (rc != PDGPU_OK) return rc;
+    }
+    for (int k = 1; k < P->K; ++k) {
+        if ((rc = launch_prep(P, w, rho, E, 0, k, st)) != PDGPU_OK) return rc;
+        if ((rc = launch_transport(P, w, rho, E, k, 0u, lslot++, true, 0, st)) != PDGPU_OK) return rc;
+    }
+    // packets parked after late_after events finish here, each with its epoch's snapshot
+    if (P->opt.late_after > 0)
+        if ((rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 1, st)) != PDGPU_OK) return rc;
+    TempParams tp;
+    tp.models = (const McModel*)(w + P->ws_models);
+    tp.dpool = (const double*)(w + P->ws_dpool);
+    tp.rho = rho;
+    tp.E = E;
+    tp.Elate = EL;
+    tp.T = temperature;
+    tp.total = P->total_cells;
+    tp.nm = P->nm;
+    tp.ns = P->ns;
+    tp.off_tinv = P->off_tinv;
+    tp.off_finv = P->off_finv;
+    int grid = (int)std::min<int64_t>((P->total_cells + 255) / 256, (int64_t)P->nsm * 8);
+    mc_temperature_kernel<<<std::max(grid, 1), 256, 0, st>>>(tp);
+    mc_finish_kernel<<<1, 1, 0, st>>>((int64_t*)(w + P->ws_stats), P->total_nphot);
+    return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
+}
+
+pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* P, const void* ws, void* stream, pdgpu_mc_stats* S) {
+    if (!P || !ws || !S) return PDGPU_INVALID_ARG;
+    int64_t h[MC_NSTAT];
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(h, (const char*)ws + P->ws_stats, sizeof(h), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    S->packets = h[ST_PACKETS];
+    S->killed = h[ST_KILLED];
+    S->escaped = h[ST_ESCAPED];
+    S->crossings = h[ST_CROSSINGS];
+    S->events = h[ST_EVENTS];
+    S->absorptions = h[ST_ABSORB];
+    S->scatterings = h[ST_SCATTER];
+    S->mrw_steps = h[ST_MRW];
+    S->status = (int32_t)h[ST_STATUS];
+    S->launches = P->K + P->npilot + (P->opt.late_after > 0 ? 1 : 0);
+    S->parked = h[ST_PARKED];
+    S->late_units = h[ST_LATE];
+    return PDGPU_OK;
+}
+
+size_t pdgpu_mctherm_workspace_bytes(int32_t nmodels, const pdgpu_model_desc* models,
+                                     const pdgpu_dust_desc* dust, const pdgpu_mc_options* options) {
+    pdgpu_mc_plan* P = nullptr;
+    if (pdgpu_mc_plan_create(nmodels, models, dust, options, &P) != PDGPU_OK) return 0;
+    size_t b = P->ws_total;
+    pdgpu_mc_plan_destroy(P);
+    return b;
+}
+
+pdgpu_status pdgpu_mctherm(int32_t nmodels, const pdgpu_model_desc* models, const pdgpu_dust_desc* dust,
+                           const pdgpu_mc_options* options, const float* rho, double* temperature,
+                           void* ws, size_t bytes, void* stream, pdgpu_mc_stats* stats) {
+    pdgpu_mc_plan* P = nullptr;
+    pdgpu_status rc = pdgpu_mc_plan_create(nmodels, models, dust, options, &P);
+    if (rc != PDGPU_OK) return rc;
+    rc = pdgpu_mc_plan_upload(P, ws, bytes, stream);
+    if (rc == PDGPU_OK) rc = pdgpu_mc_plan_run(P, rho, temperature, ws, bytes, stream);
+    pdgpu_mc_stats S;
+    memset(&S, 0, sizeof(S));
+    if (rc == PDGPU_OK) rc = pdgpu_mc_plan_stats(P, ws, stream, &S);
+    if (rc == PDGPU_OK && S.status != PDGPU_OK) rc = S.status;
+    if (stats) *stats = S;
+    pdgpu_mc_plan_destroy(P);
+    return rc;
+}
+
+}  // extern "C"

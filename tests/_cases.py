@@ -1,0 +1,44 @@
+"""Shared helpers: build small models and run the oracle on exactly the inputs the GPU
+path receives."""
+import numpy as np
+
+from oracle import orc
+from pdspy_gb300 import thermal, workloads
+
+
+def oracle_inputs(model):
+    g = model.grid
+    r, t, p = thermal.grid_arrays(g)
+    ka, ks, gg = [], [], []
+    for d in g.dust:
+        a, s, gv = thermal.opacity_on_grid(d, g.lam)
+        ka.append(a); ks.append(s); gg.append(np.zeros_like(a) if gv is None else gv)
+    sr, st = thermal._stars(g)
+    rho = thermal.stack_density(g)
+    return dict(r_edges=r, th_edges=t, ph_edges=p, rho=rho, lam_um=np.asarray(g.lam, float),
+                kabs=np.stack(ka), ksca=np.stack(ks), g=np.stack(gg), star_radius=sr,
+                star_temp=st)
+
+
+def run_oracle(model, nphot, **kw):
+    """Oracle run with the product's defaults for the epoch schedule."""
+    for k in ("nepoch", "npilot", "late_after", "mrw_eager_after"):
+        kw.setdefault(k, thermal.DEFAULTS[k])
+    return orc.mctherm(nphot=nphot, **oracle_inputs(model), **kw)
+
+
+def case(name):
+    """Small models that exercise each branch of the walk."""
+    if name == "disk_full":        # theta over [0, pi], HG scattering
+        return workloads.small_disk(nr=24, ntheta=24, mass=1e-5, g=0.6), {}
+    if name == "disk_mirror":      # theta over [0, pi/2], mirrored about the midplane
+        return workloads.small_disk(nr=20, ntheta=12, mass=1e-5, theta_max=np.pi / 2, g=0.0), {}
+    if name == "two_species_mrw":  # disk + envelope, modified random walk on
+        m = workloads.disk_envelope(nr=24, ntheta=24, mdisk=1e-3, menv=0.01, renv=1000.0)
+        return m, dict(mrw=True, mrw_gamma=2.0, mrw_tauthres=10.0, mrw_count_trigger=5)
+    if name == "spiral_3d":        # phi walls, two species
+        return workloads.spiral_disk(nr=12, ntheta=12, nphi=12, mass=1e-5), {}
+    if name == "parked":           # packets parked after 40 events, resumed at the end
+        m = workloads.small_disk(nr=24, ntheta=24, mass=1e-3, g=0.6)
+        return m, dict(late_after=40, mrw=True, mrw_count_trigger=20)
+    raise KeyError(name)

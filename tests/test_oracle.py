@@ -1,0 +1,85 @@
+"""The oracle against known answers (no GPU needed)."""
+import numpy as np
+import pytest
+
+from oracle import orc
+from pdspy_gb300 import constants as K
+from tests import _cases
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10 (Salmon et al. 2011)
+    assert orc.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert orc.philox([0xffffffff] * 4, [0xffffffff] * 2) == \
+        [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert orc.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                      [0xa4093822, 0x299f31d0]) == [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_logf_accuracy():
+    xs = np.concatenate([np.linspace(2 ** -24, 1, 2001), [1e-7, 0.5, 0.999999]]).astype(np.float32)
+    for x in xs:
+        assert abs(orc.logf(float(x)) - np.log(np.float64(x))) < 4e-7 * max(1.0, abs(np.log(x)))
+
+
+def test_sincos_accuracy():
+    for u in np.linspace(1e-6, 1 - 1e-6, 997).astype(np.float32):
+        s, c = orc.sincospif2(float(u))
+        assert abs(s - np.sin(2 * np.pi * np.float64(u))) < 3e-7
+        assert abs(c - np.cos(2 * np.pi * np.float64(u))) < 3e-7
+
+
+def _grey(nlam=200):
+    lam = np.logspace(-1, 4, nlam)
+    return lam, np.full((1, nlam), 10.0), np.zeros((1, nlam))
+
+
+def test_tables_grey_emissivity():
+    """For grey dust the row emissivity 4 pi sum kappa B dnu must approach 4 kappa sigma T^4."""
+    lam, ka, ks = _grey(400)
+    t = orc.build_tables(lam, ka, ks, None, 2 * K.R_sun, 4000.0)
+    T = 1.0 * (1e4 / 1.0) ** (np.arange(orc.ORC_NROW) / (orc.ORC_NROW - 1))
+    ok = (T > 20) & (T < 2000)
+    expect = 4 * 10.0 * K.sigma * T ** 4
+    assert np.allclose(t["F"][0][ok], expect[ok], rtol=2e-2)
+    assert np.all(np.diff(t["F"][0]) > 0)
+    cdf = t["cdf"][0]
+    assert np.all(cdf[:, -1] == 1.0) and np.all(np.diff(cdf, axis=1) >= 0)
+    assert t["star_cdf"][-1] == 1.0
+    L_bb = 4 * np.pi * (2 * K.R_sun) ** 2 * K.sigma * 4000.0 ** 4
+    assert abs(t["lum"] / L_bb - 1) < 2e-2
+
+
+def test_optically_thin_shell_temperature():
+    """Optically thin grey shell: T(r) = T* (R*/2r)^(1/2) (Bjorkman & Wood's test)."""
+    lam, ka, ks = _grey(200)
+    nr = 8
+    r = np.logspace(np.log10(2.0), np.log10(20.0), nr + 1) * K.AU
+    rho = np.full((1, nr, 1, 1), 1e-17, np.float32)
+    out = orc.mctherm(r, [0, np.pi], [0, 2 * np.pi], rho, lam, ka, ks, None, 2 * K.R_sun,
+                      4000.0, 400000, seed=1)
+    st = out["stats"]
+    assert st["escaped"] + st["killed"] == 400000
+    rc = np.sqrt(r[1:] * r[:-1])
+    T_an = 4000.0 * np.sqrt(2 * K.R_sun / (2 * rc))
+    T = out["temperature"][0, :, 0, 0]
+    assert np.all(np.abs(T / T_an - 1) < 0.05), (T, T_an)
+
+
+def test_epoch_mode_is_order_independent():
+    """Thread count must not change the int64 energy of the epoch mode."""
+    m, kw = _cases.case("disk_full")
+    a = _cases.run_oracle(m, 3000, seed=3, nthreads=1, **kw)
+    b = _cases.run_oracle(m, 3000, seed=3, nthreads=4, **kw)
+    assert np.array_equal(a["energy"], b["energy"])
+    assert np.array_equal(a["temperature"], b["temperature"])
+
+
+def test_energy_conservation_all_cases():
+    for name in ("disk_full", "disk_mirror", "spiral_3d"):
+        m, kw = _cases.case(name)
+        out = _cases.run_oracle(m, 2000, seed=0, **kw)
+        st = out["stats"]
+        assert st["escaped"] + st["killed"] == 2000, name
+        assert out["escape"].sum() == st["escaped"]
+        assert st["absorptions"] == out["energy"].sum() >> 20, name
