@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-models", type=int, default=8)
     ap.add_argument("--cpu-packets", type=int, default=100000)
+    ap.add_argument("--timelimit", type=float, default=600.0,
+                    help="device-side deadline per thermal run (s)")
     return ap.parse_args()
 
 
@@ -180,7 +182,7 @@ def main():
     dev = torch.device("cuda", local)
     models = build_models(args, rank)
     plan = thermal.ThermalPlan([m.grid for m in models], args.packets, seed=args.seed,
-                               time_launches=True, **MRW)
+                               time_launches=True, timelimit=args.timelimit, **MRW)
     host_rho = torch.from_numpy(np.concatenate(
         [thermal.stack_density(m.grid).reshape(-1) for m in models])).pin_memory()
     rho, T = plan.new_buffers()

@@ -338,6 +338,7 @@ typedef struct {
     double* sn;            /* [ntv+1] sin of the virtual theta walls  */
     double* cph; double* sph; const double* ph;  /* [np+1]           */
     double* Vr; double* Vt; double* Vp;
+    float* rf; float* muf; float* snf; float* cphf; float* sphf;  /* float copies */
 } Geo;
 
 static int make_geo(const orc_grid* g, Geo* G) {
@@ -390,11 +391,20 @@ static int make_geo(const orc_grid* g, Geo* G) {
         G->Vt[j] = G->mirror ? 2.0 * v : v;
     }
     for (int k = 0; k < g->np; ++k) G->Vp[k] = g->ph_edges[k + 1] - g->ph_edges[k];
+    G->rf = malloc(sizeof(float) * (g->nr + 1));
+    G->muf = malloc(sizeof(float) * (G->ntv + 1));
+    G->snf = malloc(sizeof(float) * (G->ntv + 1));
+    G->cphf = malloc(sizeof(float) * (g->np + 1));
+    G->sphf = malloc(sizeof(float) * (g->np + 1));
+    for (int i = 0; i <= g->nr; ++i) G->rf[i] = (float)g->r_edges[i];
+    for (int j = 0; j <= G->ntv; ++j) { G->muf[j] = (float)G->mu[j]; G->snf[j] = (float)G->sn[j]; }
+    for (int k = 0; k <= g->np; ++k) { G->cphf[k] = (float)G->cph[k]; G->sphf[k] = (float)G->sph[k]; }
     return 0;
 }
 
 static void free_geo(Geo* G) {
     free(G->mu); free(G->sn); free(G->cph); free(G->sph); free(G->Vr); free(G->Vt); free(G->Vp);
+    free(G->rf); free(G->muf); free(G->snf); free(G->cphf); free(G->sphf);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -410,7 +420,7 @@ typedef struct {
     int cell_events;
     int64_t nevents;
     int64_t ncross;
-    double dsafe;      /* lower bound of the distance to every wall of the cell */
+    float dsafe;       /* lower bound of the distance to every wall of the cell */
     uint32_t ctr[4];   /* [draw block, packet id, model, pass tag] */
     uint32_t key[2];
     uint32_t buf[4];
@@ -681,27 +691,50 @@ static float row_interp(const Ctx* X, const float* tab_s, int s, int c) {
     return tab_s[j] + w * (tab_s[j + 1] - tab_s[j]);
 }
 
-static double wall_distance(const Geo* G, const Pkt* p) {
+/* Lower bound of the distance from the packet to every wall of its cell (the safety
+ * distance and the MRW sphere radius).  The small differences that cancel near a wall
+ * (r^2 - R^2, the cone quadric rho^2 cos^2 - z^2 sin^2, the phi-plane offsets) are
+ * formed in double precision from the double position; only non-cancelling factors
+ * (r + R, |rho cos| + |z sin|) use single precision.  The result has a relative error
+ * below 1e-6, so the relative margin 4e-6 keeps it a lower bound; no square root or
+ * division runs in double precision. */
+static float wall_distance(const Geo* G, const Pkt* p) {
     double x = p->x, y = p->y, z = p->z;
-    double r = sqrt(x * x + y * y + z * z);
-    double d = r - G->r[p->ir];
-    double d2 = G->r[p->ir + 1] - r;
+    double x2 = x * x, y2 = y * y, z2 = z * z;
+    double rho2 = x2 + y2;
+    double r2 = rho2 + z2;
+    float rf = sqrtf((float)r2);
+    double Ri = G->r[p->ir], Ro = G->r[p->ir + 1];
+    float d = (float)(r2 - Ri * Ri) / (rf + G->rf[p->ir]);
+    float d2 = (float)(Ro * Ro - r2) / (rf + G->rf[p->ir + 1]);
     if (d2 < d) d = d2;
-    double rc = sqrt(x * x + y * y);
+    float rhof = sqrtf((float)rho2);
+    float zf = (float)z;
     for (int side = 0; side < 2; ++side) {
         int w = p->itv + side;
         if (w == 0 || w == G->ntv) continue;
-        double dt = fabs(rc * G->mu[w] - z * G->sn[w]);
+        float a = rhof * G->muf[w];
+        float b = zf * G->snf[w];
+        float dt;
+        if ((a > 0.0f) == (b > 0.0f)) {
+            double mu = G->mu[w], sn = G->sn[w];
+            double num = rho2 * (mu * mu) - z2 * (sn * sn);
+            float den = fabsf(a) + fabsf(b);
+            dt = den > 0.0f ? fabsf((float)num) / den : 0.0f;
+        } else {
+            dt = fabsf(a) + fabsf(b);
+        }
         if (dt < d) d = dt;
     }
     if (G->np > 1) {
         int k0 = p->ip, k1 = p->ip + 1;
-        double d0 = fabs(-x * G->sph[k0] + y * G->cph[k0]);
-        double d1 = fabs(x * G->sph[k1] - y * G->cph[k1]);
+        float d0 = (float)fabs(-x * G->sph[k0] + y * G->cph[k0]);
+        float d1 = (float)fabs(x * G->sph[k1] - y * G->cph[k1]);
         if (d0 < d) d = d0;
         if (d1 < d) d = d1;
     }
-    return d;
+    float m = d * (1.0f - 4.0e-6f);
+    return m > 0.0f ? m : 0.0f;
 }
 
 typedef struct { int64_t killed, escaped, crossings, events, absorptions, scatterings, mrw; } Cnt;
@@ -740,9 +773,10 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
          * nearest wall needs no wall solve. */
         int full = 1;
         double se = 0.0;
+        float sef = 0.0f;
         if (alpha > 0.0f) {
-            float sef = p.tau / alpha;
-            if ((double)sef < p.dsafe) { full = 0; se = (double)sef; }
+            sef = p.tau / alpha;
+            if (sef < p.dsafe) { full = 0; se = (double)sef; }
         }
         int wall = W_NONE;
         double sw = 0.0;
@@ -759,10 +793,10 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         }
         if (is_event) {
             /* interaction inside the cell */
-            p.x = p.x + se * (double)p.kx;
-            p.y = p.y + se * (double)p.ky;
-            p.z = p.z + se * (double)p.kz;
-            p.dsafe = full ? 0.0 : p.dsafe - se;
+            p.x = fma(se, (double)p.kx, p.x);
+            p.y = fma(se, (double)p.ky, p.y);
+            p.z = fma(se, (double)p.kz, p.z);
+            p.dsafe = full ? 0.0f : p.dsafe - sef;
             p.last_wall = W_NONE;
             p.cell_events += 1;
             p.nevents += 1;
@@ -772,8 +806,8 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
              * once the packet has made more than mrw_eager_after events (it is trapped). */
             if (o->mrw && (p.cell_events >= o->mrw_count_trigger ||
                            (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after))) {
-                double R0 = 0.999 * wall_distance(G, &p);
-                float R0f = (float)R0;
+                float R0f = 0.999f * wall_distance(G, &p);
+                double R0 = (double)R0f;
                 float aR = 0.0f;
                 for (int s = 0; s < ns; ++s)
                     aR = aR + X->rho[(size_t)s * G->ncell + c] *
@@ -807,9 +841,9 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                         dx = st * cs; dy = st * sn; dz = mu;
                     }
-                    p.x = p.x + R0 * (double)dx;
-                    p.y = p.y + R0 * (double)dy;
-                    p.z = p.z + R0 * (double)dz;
+                    p.x = fma(R0, (double)dx, p.x);
+                    p.y = fma(R0, (double)dy, p.y);
+                    p.z = fma(R0, (double)dz, p.z);
                     {
                         float mu = sqrtf(next_u(&p));
                         float sn, cs;
@@ -888,17 +922,16 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 }
                 p.tau = -orc_logf(next_u(&p));
             }
-            if (did_mrw) p.dsafe = 0.0;
-            else if (full) p.dsafe = 0.999999 * wall_distance(G, &p);
+            if (did_mrw || full) p.dsafe = 0.999999f * wall_distance(G, &p);
             if (p.nevents >= o->max_interactions) { cnt->killed += 1; return p.nevents; }
             if (X->pilot && X->late_after > 0 && p.nevents >= X->late_after) return p.nevents;
         } else {
             /* move to the wall and change cell */
-            p.x = p.x + sw * (double)p.kx;
-            p.y = p.y + sw * (double)p.ky;
-            p.z = p.z + sw * (double)p.kz;
+            p.x = fma(sw, (double)p.kx, p.x);
+            p.y = fma(sw, (double)p.ky, p.y);
+            p.z = fma(sw, (double)p.kz, p.z);
             p.tau = p.tau - tcell;
-            p.dsafe = 0.0;
+            p.dsafe = 0.0f;
             p.ncross += 1;
             cnt->crossings += 1;
             if (X->ccross && c >= 0) atomic_add64(&X->ccross[c], 1);

@@ -45,13 +45,13 @@ enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI
 // Saved state of a parked packet (everything in Pkt except the Philox buffer, which is
 // regenerated from the draw counter).
 struct __align__(16) ParkRec {
-    double x, y, z, dsafe;
-    float kx, ky, kz, tau;
+    double x, y, z;
+    float dsafe, kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events, nevents, ncross;
     int m, epoch;
     uint32_t pid, model, tag, draw;
-    int pad[2];
+    int pad[3];
 };
 
 struct DustTabs {       // pointers into the staged (shared or global) dust tables
@@ -102,7 +102,7 @@ struct McParams {
 
 struct Pkt {
     double x, y, z;
-    double dsafe;   // lower bound of the distance to every wall of the cell
+    float dsafe;    // lower bound of the distance to every wall of the cell
     float kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events;
@@ -254,32 +254,58 @@ __device__ __forceinline__ int cell_of(const McModel& M, const Pkt& p) {
     return (p.ir * M.nt + it) * M.np + p.ip;
 }
 
-__device__ double wall_distance(const McModel& M, const double* __restrict__ dp, const Pkt& p) {
+// Lower bound of the distance from the packet to every wall of its cell (the safety
+// distance and the MRW sphere radius).  The small differences that cancel near a wall
+// (r^2 - R^2, the cone quadric rho^2 cos^2 - z^2 sin^2, the phi-plane offsets) are formed
+// in double precision from the double position; only non-cancelling factors (r + R,
+// |rho cos| + |z sin|) use single precision.  Relative error below 1e-6, relative margin
+// 4e-6; no square root or division runs in double precision.
+__device__ float wall_distance(const McModel& M, const double* __restrict__ dp,
+                               const float* __restrict__ fg, const Pkt& p) {
+    double x = p.x, y = p.y, z = p.z;
+    double x2 = x * x, y2 = y * y, z2 = z * z;
+    double rho2 = x2 + y2;
+    double r2 = rho2 + z2;
+    float rf = sqrtf((float)r2);
     const double* R = dp + M.off_r;
+    const float* RF = fg + M.off_rf;
+    double Ri = R[p.ir], Ro = R[p.ir + 1];
+    float d = (float)(r2 - Ri * Ri) / (rf + RF[p.ir]);
+    float d2 = (float)(Ro * Ro - r2) / (rf + RF[p.ir + 1]);
+    if (d2 < d) d = d2;
+    float rhof = sqrtf((float)rho2);
+    float zf = (float)z;
     const double* MU = dp + M.off_mu;
     const double* SN = dp + M.off_sn;
-    double x = p.x, y = p.y, z = p.z;
-    double r = sqrt(x * x + y * y + z * z);
-    double d = r - R[p.ir];
-    double d2 = R[p.ir + 1] - r;
-    if (d2 < d) d = d2;
-    double rc = sqrt(x * x + y * y);
+    const float* MUF = fg + M.off_muf;
+    const float* SNF = fg + M.off_snf;
     for (int side = 0; side < 2; ++side) {
         int w = p.itv + side;
         if (w == 0 || w == M.ntv) continue;
-        double dt = fabs(rc * MU[w] - z * SN[w]);
+        float a = rhof * MUF[w];
+        float b = zf * SNF[w];
+        float dt;
+        if ((a > 0.0f) == (b > 0.0f)) {
+            double mu = MU[w], sn = SN[w];
+            double num = rho2 * (mu * mu) - z2 * (sn * sn);
+            float den = fabsf(a) + fabsf(b);
+            dt = den > 0.0f ? fabsf((float)num) / den : 0.0f;
+        } else {
+            dt = fabsf(a) + fabsf(b);
+        }
         if (dt < d) d = dt;
     }
     if (M.np > 1) {
         const double* CP = dp + M.off_cph;
         const double* SP = dp + M.off_sph;
         int k0 = p.ip, k1 = p.ip + 1;
-        double d0 = fabs(-x * SP[k0] + y * CP[k0]);
-        double d1 = fabs(x * SP[k1] - y * CP[k1]);
+        float d0 = (float)fabs(-x * SP[k0] + y * CP[k0]);
+        float d1 = (float)fabs(x * SP[k1] - y * CP[k1]);
         if (d0 < d) d = d0;
         if (d1 < d) d = d1;
     }
-    return d;
+    float m = d * (1.0f - 4.0e-6f);
+    return m > 0.0f ? m : 0.0f;
 }
 
 __device__ __forceinline__ float row_interp(const DustTabs& T, const float* tab, float q, int s) {
@@ -312,7 +338,7 @@ __device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* sta
     p.lam = mc_cdf_search(star_cdf, nl, mc_next(p.rng, k0, k1));
     p.tau = -mc_logf(mc_next(p.rng, k0, k1));
     p.x = 0.0; p.y = 0.0; p.z = 0.0;
-    p.dsafe = 0.0;
+    p.dsafe = 0.0f;
     p.ir = -1; p.itv = 0; p.ip = 0;
     p.last_wall = W_NONE;
     p.cell_events = 0;
@@ -344,9 +370,10 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
     // wall needs no wall solve (the common case in optically thick cells).
     bool full = true;
     double se = 0.0;
+    float sef = 0.0f;
     if (alpha > 0.0f) {
-        float sef = p.tau / alpha;
-        if ((double)sef < p.dsafe) { full = false; se = (double)sef; }
+        sef = p.tau / alpha;
+        if (sef < p.dsafe) { full = false; se = (double)sef; }
     }
     int wall = W_NONE;
     double sw = 0.0;
@@ -362,10 +389,10 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
         }
     }
     if (is_event) {
-        p.x = p.x + se * (double)p.kx;
-        p.y = p.y + se * (double)p.ky;
-        p.z = p.z + se * (double)p.kz;
-        p.dsafe = full ? 0.0 : p.dsafe - se;
+        p.x = fma(se, (double)p.kx, p.x);
+        p.y = fma(se, (double)p.ky, p.y);
+        p.z = fma(se, (double)p.kz, p.z);
+        p.dsafe = full ? 0.0f : p.dsafe - sef;
         p.last_wall = W_NONE;
         p.cell_events += 1;
         p.nevents += 1;
@@ -378,8 +405,8 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
         // the packet has made more than mrw_eager_after events (it is trapped).
         if (P.mrw && (p.cell_events >= P.mrw_trigger ||
                       (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after))) {
-            double R0 = 0.999 * wall_distance(M, dp, p);
-            float R0f = (float)R0;
+            float R0f = 0.999f * wall_distance(M, dp, P.fpool, p);
+            double R0 = (double)R0f;
             float2 qv[NS];
             float aR = 0.0f;
 #pragma unroll
@@ -417,9 +444,9 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     dx = st * cs; dy = st * sn; dz = mu;
                 }
-                p.x = p.x + R0 * (double)dx;
-                p.y = p.y + R0 * (double)dy;
-                p.z = p.z + R0 * (double)dz;
+                p.x = fma(R0, (double)dx, p.x);
+                p.y = fma(R0, (double)dy, p.y);
+                p.z = fma(R0, (double)dz, p.z);
                 {
                     float mu = sqrtf(mc_next(p.rng, k0, k1));
                     float sn, cs;
@@ -510,8 +537,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
             }
             p.tau = -mc_logf(mc_next(p.rng, k0, k1));
         }
-        if (did_mrw) p.dsafe = 0.0;
-        else if (full) p.dsafe = 0.999999 * wall_distance(M, dp, p);
+        if (did_mrw || full) p.dsafe = 0.999999f * wall_distance(M, dp, P.fpool, p);
         if (late) cnt.late += 1;
         if (p.nevents >= P.max_inter) {
             cnt.killed += 1;
@@ -536,11 +562,11 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
         }
         return true;
     }
-    p.x = p.x + sw * (double)p.kx;
-    p.y = p.y + sw * (double)p.ky;
-    p.z = p.z + sw * (double)p.kz;
+    p.x = fma(sw, (double)p.kx, p.x);
+    p.y = fma(sw, (double)p.ky, p.y);
+    p.z = fma(sw, (double)p.kz, p.z);
     p.tau = p.tau - tcell;
-    p.dsafe = 0.0;
+    p.dsafe = 0.0f;
     p.ncross += 1;
     cnt.crossings += 1;
     p.cell_events = 0;
@@ -1137,6 +1163,19 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
         for (int l = 0; l < nl; ++l) L += Lnu[l];
         if (!(L > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
         M.lum = L;
+        // single-precision copies of the walls for the safety distance
+        std::vector<float>& fp = P->fpool;
+        M.off_rf = (int)fp.size();
+        for (int i = 0; i <= d.nr; ++i) fp.push_back((float)dp[M.off_r + i]);
+        M.off_muf = (int)fp.size();
+        for (int j = 0; j <= M.ntv; ++j) fp.push_back((float)dp[M.off_mu + j]);
+        M.off_snf = (int)fp.size();
+        for (int j = 0; j <= M.ntv; ++j) fp.push_back((float)dp[M.off_sn + j]);
+        M.off_cphf = (int)fp.size();
+        for (int k = 0; k <= d.nphi; ++k) fp.push_back((float)dp[M.off_cph + k]);
+        M.off_sphf = (int)fp.size();
+        for (int k = 0; k <= d.nphi; ++k) fp.push_back((float)dp[M.off_sph + k]);
+        while (fp.size() % 4) fp.push_back(0.0f);
         M.off_star = (int)P->fpool.size();
         double cum = 0.0;
         for (int l = 0; l < nl; ++l) {
@@ -1332,7 +1371,9 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
         default: kern = mc_transport_kernel<4>; break;
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem_bytes) !=
-        cudaSuccess)
+            cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
         return PDGPU_CUDA_ERROR;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, P->block, P->smem_bytes) !=
