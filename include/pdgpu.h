@@ -173,6 +173,71 @@ size_t pdgpu_mctherm_workspace_bytes(int32_t nmodels, const pdgpu_model_desc* mo
                                      const pdgpu_dust_desc* dust,
                                      const pdgpu_mc_options* options);
 
+/* ------------------------------------------------------------------------- */
+/* Ray-traced images and SEDs (Model.run_image, Model.run_sed)                */
+/* ------------------------------------------------------------------------- */
+
+/* Camera of one image.  Replaces the image keywords of radmc3d.run.image
+ * (radmc3d/run.py:157-289: npix, zoomau, incl, posang, phi, nostar) as pdspy computes
+ * them in Model.run_image_radmc3d (Model.py:515-535).  Pixel (px, py) is centred at
+ * ((px - nx/2) pixel_cm, (py - ny/2) pixel_cm) in the sky plane through the origin. */
+typedef struct {
+    int32_t npix_x, npix_y;
+    double pixel_cm;                /* pixel size at the source, cm                     */
+    double incl_deg, pa_deg, phi_deg;
+    int32_t nostar;
+    int32_t max_refine;             /* sub-pixel refinement: at most 4^max_refine rays  */
+    double refine_factor;           /* sub-pixel size <= factor x smallest cell size    */
+} pdgpu_camera;
+
+typedef struct pdgpu_image_plan pdgpu_image_plan;
+
+/* Prepare one camera over one grid for nlam wavelengths; star_flux[nlam] (host, may be
+ * NULL) is the stars' flux at 1 pc, erg/s/cm^2/Hz, put into the centre pixel. */
+pdgpu_status pdgpu_image_plan_create(int32_t nr, int32_t ntheta, int32_t nphi,
+                                     const double* r_edges_cm, const double* theta_edges,
+                                     const double* phi_edges, const pdgpu_camera* camera,
+                                     int32_t nlam, const double* star_flux,
+                                     pdgpu_image_plan** plan);
+void pdgpu_image_plan_destroy(pdgpu_image_plan* plan);
+/* Workspace size, number of sub-rays and the per-pixel refinement levels (host int
+ * [npix_y][npix_x], may be NULL). */
+pdgpu_status pdgpu_image_plan_info(const pdgpu_image_plan* plan, size_t* workspace_bytes,
+                                   int64_t* nrays, int32_t* levels);
+pdgpu_status pdgpu_image_plan_upload(pdgpu_image_plan* plan, void* workspace, size_t bytes,
+                                     void* stream);
+/* Image of the per-cell extinction alpha and source S (device float [nlam][ncell], cm^-1
+ * and erg/s/cm^2/Hz/ster): device double image[nlam][ny][nx], pixel-averaged intensity
+ * at 1 pc (the unit of radmc3d/read.pyx:25-152 before pdspy's Jy conversion). */
+pdgpu_status pdgpu_image_run(pdgpu_image_plan* plan, const float* alpha, const float* S,
+                             double* image, void* workspace, size_t bytes, void* stream);
+/* Reverse-mode derivative of pdgpu_image_run: given dL/dimage (device double, as image)
+ * writes dL/dalpha and dL/dS (device double [nlam][ncell]).  No counterpart in the
+ * reference, which fits models by sampling (pdspy/utils/emcee.py:6-61). */
+pdgpu_status pdgpu_image_adjoint(pdgpu_image_plan* plan, const float* alpha, const float* S,
+                                 const double* grad_image, double* grad_alpha,
+                                 double* grad_S, void* workspace, size_t bytes, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Visibilities and chi^2 (interferometry.chisq)                              */
+/* ------------------------------------------------------------------------- */
+
+/* Direct Fourier transform of image (device float [ny][nx], Jy per pixel, pixel (i, j) at
+ * x = x0 + i dx, y = y0 + j dy radians) at nuv points (device float u, v in wavelengths):
+ * re/im (device double [nuv]) = sum F exp(-2 pi i (u x + v y)).  The chi^2
+ * sum w [(Re_d - Re)^2 + (Im_d - Im)^2] of pdspy's chisq_calc
+ * (interferometry/libinterferometry.pyx:610-633) is formed from these by the caller.
+ * Replaces galario's sampleImage in interferometry/interpolate_model.py:11-57. */
+pdgpu_status pdgpu_vis_dft(int32_t nx, int32_t ny, double x0_rad, double dx_rad, double y0_rad,
+                           double dy_rad, const float* image, int32_t nuv, const float* u,
+                           const float* v, double* re, double* im, void* stream);
+/* Adjoint of pdgpu_vis_dft: grad_image[p] = sum_k grad_re[k] cos(phi_kp) -
+ * grad_im[k] sin(phi_kp).  No counterpart in the reference. */
+pdgpu_status pdgpu_vis_dft_adjoint(int32_t nx, int32_t ny, double x0_rad, double dx_rad,
+                                   double y0_rad, double dy_rad, int32_t nuv, const float* u,
+                                   const float* v, const double* grad_re,
+                                   const double* grad_im, double* grad_image, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

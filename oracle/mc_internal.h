@@ -1,0 +1,46 @@
+/*
+ * Grid geometry shared by the thermal Monte Carlo and the ray-tracing oracle
+ * (test infrastructure only, see mcrt_oracle.h).
+ */
+#ifndef PDSPY_ORACLE_INTERNAL_H
+#define PDSPY_ORACLE_INTERNAL_H
+#include <stdint.h>
+
+#include "mcrt_oracle.h"
+
+typedef struct {
+    int nr, nt, np, ntv, mirror, ncell;
+    const double* r;       /* [nr+1]            */
+    double* mu;            /* [ntv+1] cos of the virtual theta walls  */
+    double* sn;            /* [ntv+1] sin of the virtual theta walls  */
+    double* cph; double* sph; const double* ph;  /* [np+1]           */
+    double* Vr; double* Vt; double* Vp;
+    float* rf; float* muf; float* snf; float* cphf; float* sphf;  /* float copies */
+} Geo;
+
+typedef struct {
+    double x, y, z;
+    float kx, ky, kz;
+    int ir, itv, ip;
+    int lam;
+    float tau;
+    int last_wall;
+    int cell_events;
+    int64_t nevents;
+    int64_t ncross;
+    float dsafe;       /* lower bound of the distance to every wall of the cell */
+    uint32_t ctr[4];   /* [draw block, packet id, model, pass tag] */
+    uint32_t key[2];
+    uint32_t buf[4];
+    uint32_t draw;
+} Pkt;
+
+enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI = 6 };
+
+int orc__make_geo(const orc_grid* g, Geo* G);
+void orc__free_geo(Geo* G);
+double orc__next_wall(const Geo* G, const Pkt* p, int* wall_out);
+void orc__locate_angles(const Geo* G, Pkt* p);
+int orc__cell_index(const Geo* G, const Pkt* p);
+
+#endif

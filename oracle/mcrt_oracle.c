@@ -46,6 +46,7 @@
  *  4096-row table in double precision.
  */
 #include "mcrt_oracle.h"
+#include "mc_internal.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -331,17 +332,8 @@ double orc_build_tables(const orc_dust* dust, const orc_stars* stars, double* F,
 /* ------------------------------------------------------------------------- */
 /* Grid                                                                       */
 /* ------------------------------------------------------------------------- */
-typedef struct {
-    int nr, nt, np, ntv, mirror, ncell;
-    const double* r;       /* [nr+1]            */
-    double* mu;            /* [ntv+1] cos of the virtual theta walls  */
-    double* sn;            /* [ntv+1] sin of the virtual theta walls  */
-    double* cph; double* sph; const double* ph;  /* [np+1]           */
-    double* Vr; double* Vt; double* Vp;
-    float* rf; float* muf; float* snf; float* cphf; float* sphf;  /* float copies */
-} Geo;
 
-static int make_geo(const orc_grid* g, Geo* G) {
+int orc__make_geo(const orc_grid* g, Geo* G) {
     memset(G, 0, sizeof(*G));
     G->nr = g->nr; G->nt = g->nt; G->np = g->np;
     G->ncell = g->nr * g->nt * g->np;
@@ -402,7 +394,7 @@ static int make_geo(const orc_grid* g, Geo* G) {
     return 0;
 }
 
-static void free_geo(Geo* G) {
+void orc__free_geo(Geo* G) {
     free(G->mu); free(G->sn); free(G->cph); free(G->sph); free(G->Vr); free(G->Vt); free(G->Vp);
     free(G->rf); free(G->muf); free(G->snf); free(G->cphf); free(G->sphf);
 }
@@ -410,22 +402,6 @@ static void free_geo(Geo* G) {
 /* ------------------------------------------------------------------------- */
 /* Packet                                                                     */
 /* ------------------------------------------------------------------------- */
-typedef struct {
-    double x, y, z;
-    float kx, ky, kz;
-    int ir, itv, ip;
-    int lam;
-    float tau;
-    int last_wall;
-    int cell_events;
-    int64_t nevents;
-    int64_t ncross;
-    float dsafe;       /* lower bound of the distance to every wall of the cell */
-    uint32_t ctr[4];   /* [draw block, packet id, model, pass tag] */
-    uint32_t key[2];
-    uint32_t buf[4];
-    uint32_t draw;
-} Pkt;
 
 static inline float next_u(Pkt* p) {
     uint32_t i = p->draw & 3u;
@@ -437,7 +413,6 @@ static inline float next_u(Pkt* p) {
     return u01(p->buf[i]);
 }
 
-enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI = 6 };
 
 /* Candidate acceptance: the wall the packet entered through needs a strictly positive
  * distance; any other wall accepts tiny negative roots (rounding) as zero. */
@@ -450,7 +425,7 @@ static inline int accept_root(double s, int wall, int last, double tol, double* 
     return 0;
 }
 
-static double next_wall(const Geo* G, const Pkt* p, int* wall_out) {
+double orc__next_wall(const Geo* G, const Pkt* p, int* wall_out) {
     double x = p->x, y = p->y, z = p->z;
     double kx = (double)p->kx, ky = (double)p->ky, kz = (double)p->kz;
     double kk = kx * kx + ky * ky + kz * kz;
@@ -545,7 +520,7 @@ static double next_wall(const Geo* G, const Pkt* p, int* wall_out) {
     return best;
 }
 
-static void locate_angles(const Geo* G, Pkt* p) {
+void orc__locate_angles(const Geo* G, Pkt* p) {
     double x = p->x, y = p->y, z = p->z;
     double r = sqrt(x * x + y * y + z * z);
     double ct = z / r;
@@ -569,7 +544,7 @@ static void locate_angles(const Geo* G, Pkt* p) {
     }
 }
 
-static inline int cell_index(const Geo* G, const Pkt* p) {
+int orc__cell_index(const Geo* G, const Pkt* p) {
     int it = (p->itv < G->nt) ? p->itv : (2 * G->nt - 1 - p->itv);
     return (p->ir * G->nt + it) * G->np + p->ip;
 }
@@ -765,7 +740,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         int c = -1;
         float alpha = 0.0f;
         if (p.ir >= 0) {
-            c = cell_index(G, &p);
+            c = orc__cell_index(G, &p);
             for (int s = 0; s < ns; ++s)
                 alpha = alpha + X->rho[(size_t)s * G->ncell + c] * T->kext[(size_t)s * nl + p.lam];
         }
@@ -783,7 +758,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         float tcell = 0.0f;
         int is_event = 1;
         if (full) {
-            sw = next_wall(G, &p, &wall);
+            sw = orc__next_wall(G, &p, &wall);
             tcell = alpha * (float)sw;
             is_event = tcell > p.tau;
             if (is_event) {
@@ -938,7 +913,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             p.cell_events = 0;
             switch (wall) {
                 case W_ROUT:
-                    if (p.ir < 0) { p.ir = 0; locate_angles(G, &p); }
+                    if (p.ir < 0) { p.ir = 0; orc__locate_angles(G, &p); }
                     else p.ir += 1;
                     p.last_wall = W_RIN;
                     if (p.ir >= G->nr) {
@@ -1009,7 +984,7 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
     if (dust->nlam < 2 || dust->nspec < 1 || dust->nspec > 8 || stars->nstar < 1) return 1;
     if (o->nphot < 1 || o->nphot > 4000000000LL) return 1;
     Geo G;
-    if (make_geo(grid, &G)) { free_geo(&G); return 1; }
+    if (orc__make_geo(grid, &G)) { orc__free_geo(&G); return 1; }
     Tables T;
     make_tables(dust, stars, &T, NULL, NULL);
     int ns = dust->nspec, nc = G.ncell;
@@ -1108,6 +1083,6 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
     }
     free(mass); free(qlo); free(qspan); free(D); free(Elate);
     free_tables(&T);
-    free_geo(&G);
+    orc__free_geo(&G);
     return 0;
 }

@@ -166,3 +166,53 @@ def mctherm(r_edges, th_edges, ph_edges, rho, lam_um, kabs, ksca, g, star_radius
     if cc is not None:
         out["crossings"] = cc.reshape(shape[1:])
     return out
+
+
+class Camera(C.Structure):
+    _fields_ = [("npix_x", C.c_int), ("npix_y", C.c_int), ("pixel_cm", C.c_double),
+                ("incl_deg", C.c_double), ("pa_deg", C.c_double), ("phi_deg", C.c_double),
+                ("nostar", C.c_int), ("max_refine", C.c_int), ("refine_factor", C.c_double)]
+
+
+def _grid(r_edges, th_edges, ph_edges, keep):
+    r = keep.arr(r_edges); t = keep.arr(th_edges); p = keep.arr(ph_edges)
+    return Grid(len(r) - 1, len(t) - 1, len(p) - 1, _dp(r), _dp(t), _dp(p))
+
+
+def image(r_edges, th_edges, ph_edges, alpha, S, star_flux, npix, pixel_cm, incl=0.0, pa=0.0,
+          phi=0.0, nostar=False, max_refine=6, refine_factor=0.5):
+    """Pixel-averaged intensity at 1 pc, [nlam, ny, nx]; alpha and S are [nlam, ncell]."""
+    keep = _Keep()
+    g = _grid(r_edges, th_edges, ph_edges, keep)
+    a = np.ascontiguousarray(alpha, dtype=np.float32)
+    s = np.ascontiguousarray(S, dtype=np.float32)
+    nlam = a.shape[0]
+    sf = keep.arr(np.broadcast_to(np.asarray(star_flux, dtype=np.float64), (nlam,)))
+    cam = Camera(npix, npix, pixel_cm, incl, pa, phi, int(nostar), max_refine, refine_factor)
+    out = np.zeros((nlam, npix, npix))
+    rc = lib().orc_image(C.byref(g), nlam, a.ctypes.data_as(C.c_void_p),
+                         s.ctypes.data_as(C.c_void_p), _dp(sf), C.byref(cam), _dp(out))
+    if rc:
+        raise ValueError("oracle rejected the grid")
+    return out
+
+
+def refine_levels(r_edges, th_edges, ph_edges, npix, pixel_cm, max_refine=6, refine_factor=0.5):
+    keep = _Keep()
+    g = _grid(r_edges, th_edges, ph_edges, keep)
+    cam = Camera(npix, npix, pixel_cm, 0.0, 0.0, 0.0, 1, max_refine, refine_factor)
+    lv = np.zeros(npix * npix, np.int32)
+    lib().orc_refine_levels(C.byref(g), C.byref(cam), lv.ctypes.data_as(C.c_void_p))
+    return lv.reshape(npix, npix)
+
+
+def ray_segments(r_edges, th_edges, ph_edges, npix, pixel_cm, px, py, sub, level, incl=0.0,
+                 pa=0.0, phi=0.0, cap=100000):
+    keep = _Keep()
+    g = _grid(r_edges, th_edges, ph_edges, keep)
+    cam = Camera(npix, npix, pixel_cm, incl, pa, phi, 1, 0, 0.5)
+    cells = np.zeros(cap, np.int32)
+    lens = np.zeros(cap)
+    n = lib().orc_ray_segments(C.byref(g), C.byref(cam), px, py, sub, level,
+                               cells.ctypes.data_as(C.c_void_p), _dp(lens), cap)
+    return cells[:n], lens[:n]

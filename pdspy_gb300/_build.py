@@ -23,8 +23,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags)
 UNITS = [
     ("mctherm.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("raytrace.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("dft.cu", []),
 ]
-HEADERS = ["mc_common.h", "mc_device.cuh"]
+HEADERS = ["mc_common.h", "mc_device.cuh", "mc_geom.cuh", "mc_host.h"]
 
 
 def nvcc():

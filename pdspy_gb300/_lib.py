@@ -53,6 +53,12 @@ class McLayout(C.Structure):
                 ("smem_tables", C.c_int32)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("npix_x", C.c_int32), ("npix_y", C.c_int32), ("pixel_cm", C.c_double),
+                ("incl_deg", C.c_double), ("pa_deg", C.c_double), ("phi_deg", C.c_double),
+                ("nostar", C.c_int32), ("max_refine", C.c_int32), ("refine_factor", C.c_double)]
+
+
 STATUS = {0: "ok", 1: "invalid argument", 2: "time limit reached", 3: "aborted",
           4: "packet cap", 5: "overflow", 6: "CUDA error", 7: "no device", 8: "workspace"}
 
@@ -62,6 +68,9 @@ EXPORTS = [
     "pdgpu_mc_plan_create", "pdgpu_mc_plan_destroy", "pdgpu_mc_plan_layout",
     "pdgpu_mc_plan_upload", "pdgpu_mc_plan_run", "pdgpu_mc_plan_stats",
     "pdgpu_mctherm", "pdgpu_mctherm_workspace_bytes", "pdgpu_mc_plan_launch_ms",
+    "pdgpu_image_plan_create", "pdgpu_image_plan_destroy", "pdgpu_image_plan_info",
+    "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint",
+    "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint",
 ]
 
 
@@ -107,6 +116,25 @@ def lib(build_if_missing=True):
     L.pdgpu_mctherm_workspace_bytes.restype = sz
     L.pdgpu_mctherm_workspace_bytes.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
                                                 C.POINTER(McOptions)]
+    dp = C.POINTER(C.c_double)
+    L.pdgpu_image_plan_create.restype = i32
+    L.pdgpu_image_plan_create.argtypes = [i32, i32, i32, dp, dp, dp, C.POINTER(Camera), i32, dp,
+                                          C.POINTER(vp)]
+    L.pdgpu_image_plan_destroy.restype = None
+    L.pdgpu_image_plan_destroy.argtypes = [vp]
+    L.pdgpu_image_plan_info.restype = i32
+    L.pdgpu_image_plan_info.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_int64), vp]
+    L.pdgpu_image_plan_upload.restype = i32
+    L.pdgpu_image_plan_upload.argtypes = [vp, vp, sz, vp]
+    L.pdgpu_image_run.restype = i32
+    L.pdgpu_image_run.argtypes = [vp, vp, vp, vp, vp, sz, vp]
+    L.pdgpu_image_adjoint.restype = i32
+    L.pdgpu_image_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp]
+    d = C.c_double
+    L.pdgpu_vis_dft.restype = i32
+    L.pdgpu_vis_dft.argtypes = [i32, i32, d, d, d, d, vp, i32, vp, vp, vp, vp, vp]
+    L.pdgpu_vis_dft_adjoint.restype = i32
+    L.pdgpu_vis_dft_adjoint.argtypes = [i32, i32, d, d, d, d, i32, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

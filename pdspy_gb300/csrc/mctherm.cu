@@ -37,10 +37,11 @@
 #include "../../include/pdgpu.h"
 #include "mc_common.h"
 #include "mc_device.cuh"
+#include "mc_geom.cuh"
+#include "mc_host.h"
 
 namespace {
-
-enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI = 6 };
+using namespace pdgpu;
 
 // Saved state of a parked packet (everything in Pkt except the Philox buffer, which is
 // regenerated from the draw counter).
@@ -100,213 +101,10 @@ struct McParams {
     int32_t count_stats;
 };
 
-struct Pkt {
-    double x, y, z;
-    float dsafe;    // lower bound of the distance to every wall of the cell
-    float kx, ky, kz, tau;
-    int ir, itv, ip, lam;
-    int last_wall, cell_events;
-    int nevents, ncross;
-    int m, epoch;
-    McRng rng;
-};
-
 struct Cnt {
     long long killed, escaped, crossings, events, absorb, scatter, mrw, late, parked;
     int maxev;
 };
-
-__device__ __forceinline__ bool accept_root(double s, int wall, int last, double tol, double& out) {
-    if (wall == last) {
-        if (s > tol) { out = s; return true; }
-        return false;
-    }
-    if (s >= -tol) { out = s > 0.0 ? s : 0.0; return true; }
-    return false;
-}
-
-// Distance to the wall through which the packet leaves its cell (FP64 root solves).
-__device__ double next_wall(const McModel& M, const double* __restrict__ dp, const Pkt& p,
-                            int& wall_out) {
-    const double* R = dp + M.off_r;
-    double x = p.x, y = p.y, z = p.z;
-    double kx = (double)p.kx, ky = (double)p.ky, kz = (double)p.kz;
-    double kk = kx * kx + ky * ky + kz * kz;
-    double r2 = x * x + y * y + z * z;
-    double b = x * kx + y * ky + z * kz;
-    int last = p.last_wall;
-    double best = 1.0e300;
-    int bw = W_NONE;
-    double Ro = (p.ir < 0) ? R[0] : R[p.ir + 1];
-    double tol = 1.0e-10 * Ro;
-    double cand;
-    {
-        double c = r2 - Ro * Ro;
-        double D = b * b - kk * c;
-        if (D < 0.0) D = 0.0;
-        double sq = sqrt(D);
-        double s = (b <= 0.0) ? (sq - b) / kk : -c / (b + sq);
-        if (!(last == W_ROUT && s <= tol)) { best = (s > 0.0) ? s : 0.0; bw = W_ROUT; }
-    }
-    if (p.ir < 0) { wall_out = bw; return best; }
-    if (b < 0.0) {
-        double Ri = R[p.ir];
-        double c = r2 - Ri * Ri;
-        double D = b * b - kk * c;
-        if (D >= 0.0) {
-            double s = c / (sqrt(D) - b);
-            if (accept_root(s, W_RIN, last, tol, cand) && cand < best) { best = cand; bw = W_RIN; }
-        }
-    }
-    const double* MU = dp + M.off_mu;
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-        int w = p.itv + side;
-        if (w == 0 || w == M.ntv) continue;
-        int code = side ? W_THI : W_TLO;
-        double mu = MU[w];
-        double s = 0.0;
-        bool ok = false;
-        if (mu == 0.0) {
-            if (side == 0 ? (kz > 0.0) : (kz < 0.0)) { s = -z / kz; ok = true; }
-        } else {
-            double mu2 = mu * mu;
-            double A = kz * kz - mu2 * kk;
-            double B = z * kz - mu2 * b;
-            double C = z * z - mu2 * r2;
-            bool want_plus = (side == 0) ? (mu > 0.0) : (mu < 0.0);
-            double D = B * B - A * C;
-            if (D >= 0.0) {
-                double sq = sqrt(D);
-                if (A == 0.0) {
-                    if (want_plus ? (B > 0.0) : (B < 0.0)) { s = -C / (2.0 * B); ok = true; }
-                } else {
-                    double q = (B >= 0.0) ? -(B + sq) : (sq - B);
-                    if (q != 0.0) {
-                        double sm, sp;
-                        if (B >= 0.0) { sm = q / A; sp = C / q; }
-                        else { sp = q / A; sm = C / q; }
-                        s = want_plus ? sp : sm;
-                        ok = true;
-                    }
-                }
-                if (ok) {
-                    double zs = z + s * kz;
-                    if (mu > 0.0 ? (zs < 0.0) : (zs > 0.0)) ok = false;
-                }
-            }
-        }
-        if (ok && accept_root(s, code, last, tol, cand) && cand < best) { best = cand; bw = code; }
-    }
-    if (M.np > 1) {
-        const double* CP = dp + M.off_cph;
-        const double* SP = dp + M.off_sph;
-        int k0 = p.ip, k1 = p.ip + 1;
-        double g0 = -x * SP[k0] + y * CP[k0];
-        double dg = -kx * SP[k0] + ky * CP[k0];
-        if (dg < 0.0) {
-            double s = -g0 / dg;
-            double hx = x + s * kx, hy = y + s * ky;
-            if (hx * CP[k0] + hy * SP[k0] > 0.0 && accept_root(s, W_PLO, last, tol, cand) &&
-                cand < best) { best = cand; bw = W_PLO; }
-        }
-        double h0 = x * SP[k1] - y * CP[k1];
-        double dh = kx * SP[k1] - ky * CP[k1];
-        if (dh < 0.0) {
-            double s = -h0 / dh;
-            double hx = x + s * kx, hy = y + s * ky;
-            if (hx * CP[k1] + hy * SP[k1] > 0.0 && accept_root(s, W_PHI, last, tol, cand) &&
-                cand < best) { best = cand; bw = W_PHI; }
-        }
-    }
-    wall_out = bw;
-    return best;
-}
-
-__device__ void locate_angles(const McModel& M, const double* __restrict__ dp, Pkt& p) {
-    double x = p.x, y = p.y, z = p.z;
-    double r = sqrt(x * x + y * y + z * z);
-    double ct = z / r;
-    const double* MU = dp + M.off_mu;
-    int lo = 0, hi = M.ntv;
-    while (hi - lo > 1) {
-        int mid = lo + (hi - lo) / 2;
-        if (MU[mid] >= ct) lo = mid; else hi = mid;
-    }
-    p.itv = lo;
-    if (M.np > 1) {
-        double ph = atan2(y, x);
-        if (ph < 0.0) ph += 2.0 * MC_PI;
-        const double* PH = dp + M.off_vp + M.np;  // phi edges follow the phi widths
-        int a = 0, bnd = M.np;
-        while (bnd - a > 1) {
-            int mid = a + (bnd - a) / 2;
-            if (PH[mid] <= ph) a = mid; else bnd = mid;
-        }
-        p.ip = a;
-    } else {
-        p.ip = 0;
-    }
-}
-
-__device__ __forceinline__ int cell_of(const McModel& M, const Pkt& p) {
-    int it = (p.itv < M.nt) ? p.itv : (2 * M.nt - 1 - p.itv);
-    return (p.ir * M.nt + it) * M.np + p.ip;
-}
-
-// Lower bound of the distance from the packet to every wall of its cell (the safety
-// distance and the MRW sphere radius).  The small differences that cancel near a wall
-// (r^2 - R^2, the cone quadric rho^2 cos^2 - z^2 sin^2, the phi-plane offsets) are formed
-// in double precision from the double position; only non-cancelling factors (r + R,
-// |rho cos| + |z sin|) use single precision.  Relative error below 1e-6, relative margin
-// 4e-6; no square root or division runs in double precision.
-__device__ float wall_distance(const McModel& M, const double* __restrict__ dp,
-                               const float* __restrict__ fg, const Pkt& p) {
-    double x = p.x, y = p.y, z = p.z;
-    double x2 = x * x, y2 = y * y, z2 = z * z;
-    double rho2 = x2 + y2;
-    double r2 = rho2 + z2;
-    float rf = sqrtf((float)r2);
-    const double* R = dp + M.off_r;
-    const float* RF = fg + M.off_rf;
-    double Ri = R[p.ir], Ro = R[p.ir + 1];
-    float d = (float)(r2 - Ri * Ri) / (rf + RF[p.ir]);
-    float d2 = (float)(Ro * Ro - r2) / (rf + RF[p.ir + 1]);
-    if (d2 < d) d = d2;
-    float rhof = sqrtf((float)rho2);
-    float zf = (float)z;
-    const double* MU = dp + M.off_mu;
-    const double* SN = dp + M.off_sn;
-    const float* MUF = fg + M.off_muf;
-    const float* SNF = fg + M.off_snf;
-    for (int side = 0; side < 2; ++side) {
-        int w = p.itv + side;
-        if (w == 0 || w == M.ntv) continue;
-        float a = rhof * MUF[w];
-        float b = zf * SNF[w];
-        float dt;
-        if ((a > 0.0f) == (b > 0.0f)) {
-            double mu = MU[w], sn = SN[w];
-            double num = rho2 * (mu * mu) - z2 * (sn * sn);
-            float den = fabsf(a) + fabsf(b);
-            dt = den > 0.0f ? fabsf((float)num) / den : 0.0f;
-        } else {
-            dt = fabsf(a) + fabsf(b);
-        }
-        if (dt < d) d = dt;
-    }
-    if (M.np > 1) {
-        const double* CP = dp + M.off_cph;
-        const double* SP = dp + M.off_sph;
-        int k0 = p.ip, k1 = p.ip + 1;
-        float d0 = (float)fabs(-x * SP[k0] + y * CP[k0]);
-        float d1 = (float)fabs(x * SP[k1] - y * CP[k1]);
-        if (d0 < d) d = d0;
-        if (d1 < d) d = d1;
-    }
-    float m = d * (1.0f - 4.0e-6f);
-    return m > 0.0f ? m : 0.0f;
-}
 
 __device__ __forceinline__ float row_interp(const DustTabs& T, const float* tab, float q, int s) {
     int j;
@@ -1084,73 +882,16 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
         const pdgpu_model_desc& d = models[m];
         McModel M;
         memset(&M, 0, sizeof(M));
-        if (d.nr < 1 || d.ntheta < 1 || d.nphi < 1 || !d.r_edges_cm || !d.theta_edges ||
-            !d.phi_edges || d.nstar < 1 || !d.star_radius_cm || !d.star_temperature ||
-            d.nphot < 1 || d.nphot > 4000000000LL) {
+        if (d.nstar < 1 || !d.star_radius_cm || !d.star_temperature || d.nphot < 1 ||
+            d.nphot > 4000000000LL ||
+            !append_geometry(d.nr, d.ntheta, d.nphi, d.r_edges_cm, d.theta_edges, d.phi_edges, M,
+                             P->dpool, P->fpool)) {
             delete P;
             return PDGPU_INVALID_ARG;
         }
-        if (!(d.r_edges_cm[0] > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
-        for (int i = 1; i <= d.nr; ++i)
-            if (!(d.r_edges_cm[i] > d.r_edges_cm[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
-        for (int i = 1; i <= d.ntheta; ++i)
-            if (!(d.theta_edges[i] > d.theta_edges[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
-        for (int i = 1; i <= d.nphi; ++i)
-            if (!(d.phi_edges[i] > d.phi_edges[i - 1])) { delete P; return PDGPU_INVALID_ARG; }
-        double thmax = d.theta_edges[d.ntheta];
-        if (fabs(d.theta_edges[0]) > 1e-12) { delete P; return PDGPU_INVALID_ARG; }
-        if (fabs(thmax - MC_PI) < 1e-9) M.mirror = 0;
-        else if (fabs(thmax - 0.5 * MC_PI) < 1e-9) M.mirror = 1;
-        else { delete P; return PDGPU_INVALID_ARG; }
-        if (d.nphi > 1 && (fabs(d.phi_edges[0]) > 1e-12 || fabs(d.phi_edges[d.nphi] - 2.0 * MC_PI) > 1e-9)) {
-            delete P;
-            return PDGPU_INVALID_ARG;
-        }
-        M.nr = d.nr; M.nt = d.ntheta; M.np = d.nphi;
-        M.ntv = M.mirror ? 2 * d.ntheta : d.ntheta;
-        M.ncell = d.nr * d.ntheta * d.nphi;
         M.cell_off = cell_off;
         M.model_id = m;
         M.nphot = d.nphot;
-        std::vector<double>& dp = P->dpool;
-        M.off_r = (int)dp.size();
-        for (int i = 0; i <= d.nr; ++i) dp.push_back(d.r_edges_cm[i]);
-        M.off_mu = (int)dp.size();
-        dp.resize(dp.size() + M.ntv + 1);
-        M.off_sn = (int)dp.size();
-        dp.resize(dp.size() + M.ntv + 1);
-        int nt = d.ntheta;
-        for (int j = 0; j <= nt; ++j) {
-            double th = d.theta_edges[j];
-            double mv = cos(th), sv = sin(th);
-            if (fabs(th - 0.5 * MC_PI) < 1e-12) { mv = 0.0; sv = 1.0; }
-            if (j == 0) { mv = 1.0; sv = 0.0; }
-            if (!M.mirror && j == nt) { mv = -1.0; sv = 0.0; }
-            dp[M.off_mu + j] = mv;
-            dp[M.off_sn + j] = sv;
-        }
-        if (M.mirror)
-            for (int j = 0; j < nt; ++j) {
-                dp[M.off_mu + 2 * nt - j] = -dp[M.off_mu + j];
-                dp[M.off_sn + 2 * nt - j] = dp[M.off_sn + j];
-            }
-        M.off_cph = (int)dp.size();
-        for (int k = 0; k <= d.nphi; ++k) dp.push_back(cos(d.phi_edges[k]));
-        M.off_sph = (int)dp.size();
-        for (int k = 0; k <= d.nphi; ++k) dp.push_back(sin(d.phi_edges[k]));
-        M.off_vr = (int)dp.size();
-        for (int i = 0; i < d.nr; ++i) {
-            double r0 = d.r_edges_cm[i], r1 = d.r_edges_cm[i + 1];
-            dp.push_back((r1 * r1 * r1 - r0 * r0 * r0) / 3.0);
-        }
-        M.off_vt = (int)dp.size();
-        for (int j = 0; j < nt; ++j) {
-            double v = dp[M.off_mu + j] - dp[M.off_mu + j + 1];
-            dp.push_back(M.mirror ? 2.0 * v : v);
-        }
-        M.off_vp = (int)dp.size();
-        for (int k = 0; k < d.nphi; ++k) dp.push_back(d.phi_edges[k + 1] - d.phi_edges[k]);
-        for (int k = 0; k <= d.nphi; ++k) dp.push_back(d.phi_edges[k]);  // edges after widths
         // stellar spectrum
         std::vector<double> Lnu(nl, 0.0);
         for (int s = 0; s < d.nstar; ++s) {
@@ -1163,19 +904,6 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
         for (int l = 0; l < nl; ++l) L += Lnu[l];
         if (!(L > 0.0)) { delete P; return PDGPU_INVALID_ARG; }
         M.lum = L;
-        // single-precision copies of the walls for the safety distance
-        std::vector<float>& fp = P->fpool;
-        M.off_rf = (int)fp.size();
-        for (int i = 0; i <= d.nr; ++i) fp.push_back((float)dp[M.off_r + i]);
-        M.off_muf = (int)fp.size();
-        for (int j = 0; j <= M.ntv; ++j) fp.push_back((float)dp[M.off_mu + j]);
-        M.off_snf = (int)fp.size();
-        for (int j = 0; j <= M.ntv; ++j) fp.push_back((float)dp[M.off_sn + j]);
-        M.off_cphf = (int)fp.size();
-        for (int k = 0; k <= d.nphi; ++k) fp.push_back((float)dp[M.off_cph + k]);
-        M.off_sphf = (int)fp.size();
-        for (int k = 0; k <= d.nphi; ++k) fp.push_back((float)dp[M.off_sph + k]);
-        while (fp.size() % 4) fp.push_back(0.0f);
         M.off_star = (int)P->fpool.size();
         double cum = 0.0;
         for (int l = 0; l < nl; ++l) {

@@ -42,3 +42,23 @@ def case(name):
         m = workloads.small_disk(nr=24, ntheta=24, mass=1e-3, g=0.6)
         return m, dict(late_after=40, mrw=True, mrw_count_trigger=20)
     raise KeyError(name)
+
+
+def image_model(kind="disk", nr=16, ntheta=16, nphi=1, mass=1e-3, lam=None):
+    """Small model with an analytic temperature (T = 150 K (r/au)^-0.5 per species)."""
+    import numpy as np
+    if kind == "disk":
+        m = workloads.small_disk(nr=nr, ntheta=ntheta, mass=mass, lam_um=lam)
+    elif kind == "mirror":
+        m = workloads.small_disk(nr=nr, ntheta=ntheta, mass=mass, theta_max=np.pi / 2, lam_um=lam)
+    elif kind == "spiral":
+        m = workloads.spiral_disk(nr=nr, ntheta=ntheta, nphi=nphi, mass=mass)
+    elif kind == "envelope":
+        m = workloads.disk_envelope(nr=nr, ntheta=ntheta, mdisk=mass, menv=0.01, renv=1000.0)
+    else:
+        raise KeyError(kind)
+    g = m.grid
+    rr = np.meshgrid(g.r, g.theta, g.phi, indexing="ij")[0]
+    T = 150.0 * rr ** -0.5
+    g.temperature = [T * (1.0 + 0.1 * i) for i in range(len(g.density))]
+    return m
