@@ -38,46 +38,61 @@ __device__ __forceinline__ bool accept_root(double s, int wall, int last, double
     return false;
 }
 
-// Distance to the wall through which the packet leaves its cell (FP64 root solves).
-__device__ inline double next_wall(const McModel& M, const double* __restrict__ dp, const Pkt& p,
-                            int& wall_out) {
+// Quantities shared by the wall candidates of one step.
+struct WallFrame {
+    double x, y, z, kx, ky, kz, kk, r2, b, tol;
+    int last;
+};
+
+__device__ __forceinline__ void wall_frame(const McModel& M, const double* __restrict__ dp,
+                                           const Pkt& p, WallFrame& f) {
     const double* R = dp + M.off_r;
-    double x = p.x, y = p.y, z = p.z;
-    double kx = (double)p.kx, ky = (double)p.ky, kz = (double)p.kz;
-    double kk = kx * kx + ky * ky + kz * kz;
-    double r2 = x * x + y * y + z * z;
-    double b = x * kx + y * ky + z * kz;
-    int last = p.last_wall;
-    double best = 1.0e300;
-    int bw = W_NONE;
+    f.x = p.x; f.y = p.y; f.z = p.z;
+    f.kx = (double)p.kx; f.ky = (double)p.ky; f.kz = (double)p.kz;
+    f.kk = f.kx * f.kx + f.ky * f.ky + f.kz * f.kz;
+    f.r2 = f.x * f.x + f.y * f.y + f.z * f.z;
+    f.b = f.x * f.kx + f.y * f.ky + f.z * f.kz;
+    f.last = p.last_wall;
     double Ro = (p.ir < 0) ? R[0] : R[p.ir + 1];
-    double tol = 1.0e-10 * Ro;
-    double cand;
-    {
+    f.tol = 1.0e-10 * Ro;
+}
+
+// Exit distance through wall candidate k (0 outer sphere, 1 inner sphere, 2 lower cone,
+// 3 upper cone, 4 lower phi half-plane, 5 upper phi half-plane), FP64.  Returns false if
+// the packet cannot leave through that wall.
+__device__ inline bool wall_candidate(const McModel& M, const double* __restrict__ dp,
+                                      const Pkt& p, const WallFrame& f, int k, double& out) {
+    const double x = f.x, y = f.y, z = f.z, kx = f.kx, ky = f.ky, kz = f.kz;
+    const double kk = f.kk, r2 = f.r2, b = f.b, tol = f.tol;
+    const int last = f.last;
+    const double* R = dp + M.off_r;
+    if (k == 0) {
+        double Ro = (p.ir < 0) ? R[0] : R[p.ir + 1];
         double c = r2 - Ro * Ro;
         double D = b * b - kk * c;
         if (D < 0.0) D = 0.0;
         double sq = sqrt(D);
         double s = (b <= 0.0) ? (sq - b) / kk : -c / (b + sq);
-        if (!(last == W_ROUT && s <= tol)) { best = (s > 0.0) ? s : 0.0; bw = W_ROUT; }
+        if (last == W_ROUT && s <= tol) return false;
+        out = (s > 0.0) ? s : 0.0;
+        return true;
     }
-    if (p.ir < 0) { wall_out = bw; return best; }
-    if (b < 0.0) {
+    if (p.ir < 0) return false;
+    if (k == 1) {
+        if (!(b < 0.0)) return false;
         double Ri = R[p.ir];
         double c = r2 - Ri * Ri;
         double D = b * b - kk * c;
-        if (D >= 0.0) {
-            double s = c / (sqrt(D) - b);
-            if (accept_root(s, W_RIN, last, tol, cand) && cand < best) { best = cand; bw = W_RIN; }
-        }
+        if (!(D >= 0.0)) return false;
+        double s = c / (sqrt(D) - b);
+        return accept_root(s, W_RIN, last, tol, out);
     }
-    const double* MU = dp + M.off_mu;
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
+    if (k == 2 || k == 3) {
+        const int side = k - 2;
         int w = p.itv + side;
-        if (w == 0 || w == M.ntv) continue;
+        if (w == 0 || w == M.ntv) return false;
         int code = side ? W_THI : W_TLO;
-        double mu = MU[w];
+        double mu = dp[M.off_mu + w];
         double s = 0.0;
         bool ok = false;
         if (mu == 0.0) {
@@ -109,27 +124,47 @@ __device__ inline double next_wall(const McModel& M, const double* __restrict__ 
                 }
             }
         }
-        if (ok && accept_root(s, code, last, tol, cand) && cand < best) { best = cand; bw = code; }
+        return ok && accept_root(s, code, last, tol, out);
     }
-    if (M.np > 1) {
-        const double* CP = dp + M.off_cph;
-        const double* SP = dp + M.off_sph;
-        int k0 = p.ip, k1 = p.ip + 1;
+    if (M.np <= 1) return false;
+    const double* CP = dp + M.off_cph;
+    const double* SP = dp + M.off_sph;
+    if (k == 4) {
+        int k0 = p.ip;
         double g0 = -x * SP[k0] + y * CP[k0];
         double dg = -kx * SP[k0] + ky * CP[k0];
-        if (dg < 0.0) {
-            double s = -g0 / dg;
-            double hx = x + s * kx, hy = y + s * ky;
-            if (hx * CP[k0] + hy * SP[k0] > 0.0 && accept_root(s, W_PLO, last, tol, cand) &&
-                cand < best) { best = cand; bw = W_PLO; }
-        }
-        double h0 = x * SP[k1] - y * CP[k1];
-        double dh = kx * SP[k1] - ky * CP[k1];
-        if (dh < 0.0) {
-            double s = -h0 / dh;
-            double hx = x + s * kx, hy = y + s * ky;
-            if (hx * CP[k1] + hy * SP[k1] > 0.0 && accept_root(s, W_PHI, last, tol, cand) &&
-                cand < best) { best = cand; bw = W_PHI; }
+        if (!(dg < 0.0)) return false;
+        double s = -g0 / dg;
+        double hx = x + s * kx, hy = y + s * ky;
+        return hx * CP[k0] + hy * SP[k0] > 0.0 && accept_root(s, W_PLO, last, tol, out);
+    }
+    int k1 = p.ip + 1;
+    double h0 = x * SP[k1] - y * CP[k1];
+    double dh = kx * SP[k1] - ky * CP[k1];
+    if (!(dh < 0.0)) return false;
+    double s = -h0 / dh;
+    double hx = x + s * kx, hy = y + s * ky;
+    return hx * CP[k1] + hy * SP[k1] > 0.0 && accept_root(s, W_PHI, last, tol, out);
+}
+
+__device__ __forceinline__ int wall_code(int k) {
+    return k == 0 ? W_ROUT : k == 1 ? W_RIN : k == 2 ? W_TLO : k == 3 ? W_THI : k == 4 ? W_PLO : W_PHI;
+}
+
+// Distance to the wall through which the packet leaves its cell: the first candidate (in
+// the order above) with the smallest exit distance.
+__device__ inline double next_wall(const McModel& M, const double* __restrict__ dp, const Pkt& p,
+                                   int& wall_out) {
+    WallFrame f;
+    wall_frame(M, dp, p, f);
+    double best = 1.0e300;
+    int bw = W_NONE;
+    const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
+    for (int k = 0; k < nk; ++k) {
+        double s;
+        if (wall_candidate(M, dp, p, f, k, s) && s < best) {
+            best = s;
+            bw = wall_code(k);
         }
     }
     wall_out = bw;

@@ -106,22 +106,126 @@ struct Cnt {
     int maxev;
 };
 
-__device__ __forceinline__ float row_interp(const DustTabs& T, const float* tab, float q, int s) {
+// Execution policies of the transport step.
+//
+// LanePol: one packet per thread (the epoch launches).
+// WarpPol: one packet per warp, its state replicated in all 32 lanes (the continuation of
+// long parked packets, whose sequential chains set the run time).  The lanes share the
+// work that is independent within a step: a window of 32 Philox blocks is generated at
+// once (lane i holds block base+i, a draw is a shuffle), table searches count the entries
+// <= the key with ballots, and the six wall candidates are solved by lanes 0..5 and reduced
+// with the serial tie-break (first candidate with the smallest distance).  Every result is
+// identical to the per-thread code; memory side effects are issued by lane 0 only.
+struct LanePol {
+    __device__ __forceinline__ float next(McRng& r, uint32_t k0, uint32_t k1) {
+        return mc_next(r, k0, k1);
+    }
+    __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
+        return mc_cdf_search(c, n, u);
+    }
+    __device__ __forceinline__ void row(const float* F, float q, int& j, float& w) const {
+        mc_row_search(F, q, j, w);
+    }
+    __device__ __forceinline__ double wall(const McModel& M, const double* dp, const Pkt& p,
+                                           int& w) const {
+        return next_wall(M, dp, p, w);
+    }
+    __device__ __forceinline__ bool leader() const { return true; }
+};
+
+struct WarpPol {
+    int lane;
+    bool valid;
+    uint32_t base, b0, b1, b2, b3;
+    __device__ __forceinline__ explicit WarpPol(int l) : lane(l), valid(false), base(0) {}
+    __device__ __forceinline__ float next(McRng& r, uint32_t k0, uint32_t k1) {
+        uint32_t blk = r.draw >> 2;
+        if (!valid || blk < base || blk - base >= 32u) {
+            base = blk;
+            uint4 o = philox4x32_10(make_uint4(blk + (uint32_t)lane, r.pid, r.model, r.tag), k0, k1);
+            b0 = o.x; b1 = o.y; b2 = o.z; b3 = o.w;
+            valid = true;
+        }
+        uint32_t i = r.draw & 3u;
+        uint32_t x = (i == 0u) ? b0 : (i == 1u) ? b1 : (i == 2u) ? b2 : b3;
+        x = __shfl_sync(0xffffffffu, x, (int)(blk - base));
+        r.draw += 1u;
+        return mc_u01(x);
+    }
+    // number of entries <= u of a non-decreasing table == smallest index with c > u
+    __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
+        int cnt = 0;
+        for (int b = 0; b < n; b += 32) {
+            int l = b + lane;
+            bool le = (l < n) && (c[l] <= u);
+            cnt += __popc(__ballot_sync(0xffffffffu, le));
+        }
+        return cnt;
+    }
+    __device__ __forceinline__ void row(const float* F, float q, int& j, float& w) const {
+        int cnt = 0;
+#pragma unroll
+        for (int b = 0; b < MC_NROW; b += 32) cnt += __popc(__ballot_sync(0xffffffffu, F[b + lane] <= q));
+        if (cnt == 0) {
+            j = 0;
+            w = 0.0f;
+        } else if (cnt == MC_NROW) {
+            j = MC_NROW - 2;
+            w = 1.0f;
+        } else {
+            j = cnt - 1;
+            w = (q - F[j]) / (F[j + 1] - F[j]);
+            if (w < 0.0f) w = 0.0f;
+            if (w > 1.0f) w = 1.0f;
+        }
+    }
+    __device__ __forceinline__ double wall(const McModel& M, const double* dp, const Pkt& p,
+                                           int& w) const {
+        WallFrame f;
+        wall_frame(M, dp, p, f);
+        const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
+        double s = 1.0e300;
+        int k = lane;
+        if (lane < nk) {
+            double v;
+            if (!wall_candidate(M, dp, p, f, lane, v)) k = 64 + lane;
+            else s = v;
+        } else {
+            k = 64 + lane;
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            double so = __shfl_xor_sync(0xffffffffu, s, o);
+            int ko = __shfl_xor_sync(0xffffffffu, k, o);
+            if (so < s || (so == s && ko < k)) { s = so; k = ko; }
+        }
+        s = __shfl_sync(0xffffffffu, s, 0);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        w = (k < 64) ? wall_code(k) : W_NONE;
+        return (k < 64) ? s : 1.0e300;
+    }
+    __device__ __forceinline__ bool leader() const { return lane == 0; }
+};
+
+template <class Pol>
+__device__ __forceinline__ float row_interp(Pol& pol, const DustTabs& T, const float* tab, float q,
+                                            int s) {
     int j;
     float w;
-    mc_row_search(T.F + s * MC_NROW, q, j, w);
+    pol.row(T.F + s * MC_NROW, q, j, w);
     return tab[j] + w * (tab[j + 1] - tab[j]);
 }
 
-__device__ __forceinline__ int reemit_lambda(const DustTabs& T, int nl, Pkt& p, uint32_t k0,
-                                             uint32_t k1, float2 q, int s) {
-    float uq = mc_next(p.rng, k0, k1);
+template <class Pol>
+__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, Pkt& p,
+                                             uint32_t k0, uint32_t k1, float2 q, int s) {
+    float uq = pol.next(p.rng, k0, k1);
     float qq = q.x + uq * q.y;
     int j;
     float w;
-    mc_row_search(T.F + s * MC_NROW, qq, j, w);
-    int row = j + ((mc_next(p.rng, k0, k1) < w) ? 1 : 0);
-    return mc_cdf_search(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, mc_next(p.rng, k0, k1));
+    pol.row(T.F + s * MC_NROW, qq, j, w);
+    int row = j + ((pol.next(p.rng, k0, k1) < w) ? 1 : 0);
+    return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, pol.next(p.rng, k0, k1));
 }
 
 __device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* star_cdf, int nl,
@@ -146,8 +250,8 @@ __device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* sta
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
 // has left the grid or was killed.
-template <int NS>
-__device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) {
+template <int NS, class Pol>
+__device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, Pol& pol) {
     const McModel& M = P.models[p.m];
     const double* __restrict__ dp = P.dpool;
     const int nl = P.nl;
@@ -178,7 +282,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
     float tcell = 0.0f;
     bool is_event = true;
     if (full) {
-        sw = next_wall(M, dp, p, wall);
+        sw = pol.wall(M, dp, p, wall);
         tcell = alpha * (float)sw;
         is_event = tcell > p.tau;
         if (is_event) {
@@ -210,11 +314,11 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
                 qv[s] = qa[base + (int64_t)s * M.ncell + c];
-                aR = aR + rh[s] * row_interp(T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
             }
             if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
                 did_mrw = true;
-                float uy = mc_next(p.rng, k0, k1);
+                float uy = pol.next(p.rng, k0, k1);
                 float f = uy * (float)(MC_NMRW - 1);
                 int i = (int)f;
                 if (i > MC_NMRW - 2) i = MC_NMRW - 2;
@@ -225,20 +329,20 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                 float aP = 0.0f;
 #pragma unroll
                 for (int s = 0; s < NS; ++s) {
-                    kp[s] = rh[s] * row_interp(T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                    kp[s] = rh[s] * row_interp(pol, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
                     aP = aP + kp[s];
                     float units_f = kp[s] * ell * 1048576.0f + 0.5f;
                     if (units_f > 9.0e18f) units_f = 9.0e18f;
                     long long units = (long long)units_f;
-                    if (units > 0)
+                    if (units > 0 && pol.leader())
                         atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
                                   (unsigned long long)units);
                 }
                 float dx, dy, dz;
                 {
-                    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+                    float mu = 2.0f * pol.next(p.rng, k0, k1) - 1.0f;
                     float sn, cs;
-                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     dx = st * cs; dy = st * sn; dz = mu;
                 }
@@ -246,16 +350,16 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                 p.y = fma(R0, (double)dy, p.y);
                 p.z = fma(R0, (double)dz, p.z);
                 {
-                    float mu = sqrtf(mc_next(p.rng, k0, k1));
+                    float mu = sqrtf(pol.next(p.rng, k0, k1));
                     float sn, cs;
-                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
                     float kx = dx, ky = dy, kz = dz;
                     mc_rotate(kx, ky, kz, mu, cs, sn);
                     p.kx = kx; p.ky = ky; p.kz = kz;
                 }
                 int sp = 0;
                 if (NS > 1) {
-                    float us = mc_next(p.rng, k0, k1) * aP;
+                    float us = pol.next(p.rng, k0, k1) * aP;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -268,21 +372,21 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
 #pragma unroll
                 for (int s = 1; s < NS; ++s)
                     if (s == sp) qs = qv[s];
-                p.lam = reemit_lambda(T, nl, p, k0, k1, qs, sp);
-                p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+                p.lam = reemit_lambda(pol, T, nl, p, k0, k1, qs, sp);
+                p.tau = -mc_logf(pol.next(p.rng, k0, k1));
                 p.cell_events = 0;
                 cnt.mrw += 1;
             }
         }
         if (!did_mrw) {
-            float ua = mc_next(p.rng, k0, k1);
+            float ua = pol.next(p.rng, k0, k1);
             float asca = 0.0f;
 #pragma unroll
             for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + p.lam];
             if (ua * alpha < asca) {
                 int sp = 0;
                 if (NS > 1) {
-                    float us = mc_next(p.rng, k0, k1) * asca;
+                    float us = pol.next(p.rng, k0, k1) * asca;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -292,7 +396,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                     }
                 }
                 float g = T.g[sp * nl + p.lam];
-                float umu = mc_next(p.rng, k0, k1);
+                float umu = pol.next(p.rng, k0, k1);
                 float mu;
                 if (fabsf(g) < 1.0e-4f) {
                     mu = 2.0f * umu - 1.0f;
@@ -303,7 +407,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                     if (mu > 1.0f) mu = 1.0f;
                 }
                 float sn, cs;
-                mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
                 mc_rotate(p.kx, p.ky, p.kz, mu, cs, sn);
                 cnt.scatter += 1;
             } else {
@@ -312,7 +416,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                     float aabs = 0.0f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + p.lam];
-                    float us = mc_next(p.rng, k0, k1) * aabs;
+                    float us = pol.next(p.rng, k0, k1) * aabs;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -322,18 +426,18 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
                     }
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
-                atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
-                p.lam = reemit_lambda(T, nl, p, k0, k1, qa[idx], sp);
+                if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
+                p.lam = reemit_lambda(pol, T, nl, p, k0, k1, qa[idx], sp);
                 {
-                    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+                    float mu = 2.0f * pol.next(p.rng, k0, k1) - 1.0f;
                     float sn, cs;
-                    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     p.kx = st * cs; p.ky = st * sn; p.kz = mu;
                 }
                 cnt.absorb += 1;
             }
-            p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+            p.tau = -mc_logf(pol.next(p.rng, k0, k1));
         }
         if (did_mrw || full) p.dsafe = 0.999999f * wall_distance(M, dp, P.fpool, p);
         if (late) cnt.late += 1;
@@ -375,7 +479,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt) 
             p.last_wall = W_RIN;
             if (p.ir >= M.nr) {
                 cnt.escaped += 1;
-                if (P.escape) atomicAdd((unsigned long long*)(P.escape + (int64_t)p.m * nl + p.lam), 1ull);
+                if (P.escape && pol.leader()) atomicAdd((unsigned long long*)(P.escape + (int64_t)p.m * nl + p.lam), 1ull);
                 return false;
             }
             break;
@@ -443,36 +547,9 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
     Pkt p;
     bool active = false;
     unsigned iter = 0;
-    // Continuations are long by construction: spread them one per warp over the SMs
-    // (packet g -> block g mod grid, then warp, then lane) so that they do not share a
-    // warp's issue slots; the epoch launches use the dynamic warp-aggregated queue.
-    const int wpb = blockDim.x >> 5;
-    const int warp_in_block = threadIdx.x >> 5;
-    long long kstatic = 0;
+    LanePol lanepol;
     for (;;) {
         if (s_stop) break;
-        if (P.phase == 1) {
-            if (!active) {
-                long long g = (long long)blockIdx.x +
-                              (long long)gridDim.x * (warp_in_block + (long long)wpb * (lane + 32 * kstatic));
-                if (g < total) {
-                    ++kstatic;
-                    const ParkRec r = P.park[g];
-                    p.x = r.x; p.y = r.y; p.z = r.z; p.dsafe = r.dsafe;
-                    p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
-                    p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
-                    p.last_wall = r.last_wall; p.cell_events = r.cell_events;
-                    p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
-                    p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag; p.rng.draw = r.draw;
-                    if (p.rng.draw & 3u) {
-                        uint4 o = philox4x32_10(make_uint4(p.rng.draw >> 2, p.rng.pid, p.rng.model, p.rng.tag),
-                                                P.key0, P.key1);
-                        p.rng.b0 = o.x; p.rng.b1 = o.y; p.rng.b2 = o.z; p.rng.b3 = o.w;
-                    }
-                    active = true;
-                }
-            }
-        } else {
         unsigned need = __ballot_sync(0xffffffffu, !active);
         if (need) {
             int n = __popc(need);
@@ -499,10 +576,9 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
                 }
             }
         }
-        }
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
-            active = mc_step<NS>(p, P, T, cnt);
+            active = mc_step<NS>(p, P, T, cnt, lanepol);
             if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
         }
         if (((++iter) & 4095u) == 0u) {
@@ -546,6 +622,88 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
         atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
         atomicMax((unsigned long long*)(L + 2), (unsigned long long)mx);
         if (pk) atomicAdd((unsigned long long*)(L + 3), (unsigned long long)pk);
+    }
+}
+
+// Continuation of parked packets: one packet per warp (WarpPol), taken from a queue.
+template <int NS>
+__global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
+    extern __shared__ float4 smem4[];
+    float* sm = reinterpret_cast<float*>(smem4);
+    __shared__ int s_stop;
+    __shared__ long long s_total;
+    if (threadIdx.x == 0) {
+        s_stop = (*(volatile long long*)(P.stats + ST_STOP) != 0) ? 1 : 0;
+        long long c = (long long)*(volatile unsigned long long*)P.park_count;
+        s_total = c < P.park_cap ? c : P.park_cap;
+        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
+    }
+    const float* tab = P.fpool;
+    if (P.use_smem) {
+        const float4* src = reinterpret_cast<const float4*>(P.fpool);
+        int n4 = (P.dust_floats + 3) / 4;
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) smem4[i] = __ldg(src + i);
+        tab = sm;
+    }
+    __syncthreads();
+    const long long total = s_total;
+    DustTabs T;
+    T.kabs = tab + P.o_kabs; T.ksca = tab + P.o_ksca; T.kext = tab + P.o_kext; T.g = tab + P.o_g;
+    T.F = tab + P.o_F; T.cdf = tab + P.o_cdf; T.kP = tab + P.o_kP; T.kR = tab + P.o_kR;
+    T.mrw = tab + P.o_mrw;
+    const int lane = threadIdx.x & 31;
+    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool stop = s_stop != 0;
+    unsigned iter = 0;
+    while (!stop) {
+        unsigned long long g = 0;
+        if (lane == 0) g = atomicAdd(P.queue, 1ull);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if ((long long)g >= total) break;
+        const ParkRec r = P.park[g];
+        Pkt p;
+        p.x = r.x; p.y = r.y; p.z = r.z; p.dsafe = r.dsafe;
+        p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
+        p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
+        p.last_wall = r.last_wall; p.cell_events = r.cell_events;
+        p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
+        p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag; p.rng.draw = r.draw;
+        WarpPol pol(lane);
+        bool alive = true;
+        while (alive) {
+            alive = mc_step<NS>(p, P, T, cnt, pol);
+            if (((++iter) & 4095u) == 0u) {
+                int st = 0;
+                if (lane == 0) {
+                    if (*(volatile long long*)(P.stats + ST_STOP) != 0) st = 1;
+                    if (P.abort_flag && *P.abort_flag != 0) {
+                        atomicCAS((unsigned long long*)(P.stats + ST_STATUS), 0ull, (unsigned long long)PDGPU_ABORTED);
+                        st = 1;
+                    }
+                    if (P.deadline_ns > 0 &&
+                        (long long)globaltimer() - P.stats[ST_T0] > P.deadline_ns) {
+                        atomicCAS((unsigned long long*)(P.stats + ST_STATUS), 0ull, (unsigned long long)PDGPU_TIMEOUT);
+                        st = 1;
+                    }
+                    if (st) atomicExch((unsigned long long*)(P.stats + ST_STOP), 1ull);
+                }
+                st = __shfl_sync(0xffffffffu, st, 0);
+                if (st) { stop = true; break; }
+            }
+        }
+        if (p.nevents > cnt.maxev) cnt.maxev = p.nevents;
+    }
+    // every lane followed the same packets: only lane 0 reports
+    if (lane == 0) {
+        const long long v[9] = {cnt.killed, cnt.escaped, cnt.crossings, cnt.events, cnt.absorb,
+                                cnt.scatter, cnt.mrw, cnt.late, cnt.parked};
+        const int slot[9] = {ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
+                             ST_MRW, ST_LATE, ST_PARKED};
+        for (int i = 0; i < 9; ++i)
+            if (v[i]) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)v[i]);
+        int64_t* L = P.stats + MC_LSTAT + 4 * P.lslot;
+        atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
+        atomicMax((unsigned long long*)(L + 2), (unsigned long long)cnt.maxev);
     }
 }
 
@@ -1092,11 +1250,20 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.count_stats = final_pass ? 1 : 0;
     if (prm.total <= 0) return PDGPU_OK;
     void (*kern)(McParams) = nullptr;
-    switch (P->ns) {
-        case 1: kern = mc_transport_kernel<1>; break;
-        case 2: kern = mc_transport_kernel<2>; break;
-        case 3: kern = mc_transport_kernel<3>; break;
-        default: kern = mc_transport_kernel<4>; break;
+    if (phase == 0) {
+        switch (P->ns) {
+            case 1: kern = mc_transport_kernel<1>; break;
+            case 2: kern = mc_transport_kernel<2>; break;
+            case 3: kern = mc_transport_kernel<3>; break;
+            default: kern = mc_transport_kernel<4>; break;
+        }
+    } else {
+        switch (P->ns) {
+            case 1: kern = mc_continue_kernel<1>; break;
+            case 2: kern = mc_continue_kernel<2>; break;
+            case 3: kern = mc_continue_kernel<3>; break;
+            default: kern = mc_continue_kernel<4>; break;
+        }
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem_bytes) !=
             cudaSuccess ||
