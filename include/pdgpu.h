@@ -52,7 +52,8 @@ enum {
     PDGPU_OVERFLOW = 5,      /* a fixed-point accumulator would overflow                */
     PDGPU_CUDA_ERROR = 6,    /* a CUDA runtime call failed                              */
     PDGPU_NO_DEVICE = 7,     /* no usable sm_103 device                                 */
-    PDGPU_WORKSPACE = 8      /* workspace missing, too small or not uploaded            */
+    PDGPU_WORKSPACE = 8,     /* workspace missing, too small or not uploaded            */
+    PDGPU_TOO_LARGE = 9      /* needs more than the library's static scratch            */
 };
 
 /* Library identity. Replaces nothing in the reference (version probe for the binding). */
@@ -172,6 +173,24 @@ pdgpu_status pdgpu_mctherm(int32_t nmodels, const pdgpu_model_desc* models,
 size_t pdgpu_mctherm_workspace_bytes(int32_t nmodels, const pdgpu_model_desc* models,
                                      const pdgpu_dust_desc* dust,
                                      const pdgpu_mc_options* options);
+
+/* Scratch-free thermal run, for callers that cannot allocate device memory: host codes
+ * whose GPU memory is owned by another runtime or pool (a Fortran or C walker sharing the
+ * GPU with an MCMC framework, code running where cudaMalloc is not permitted).  No
+ * counterpart in the reference.  Same arguments and results as pdgpu_mctherm except that
+ * the workspace is a file-scope device array of PDGPU_STATIC_WORKSPACE_BYTES held by every
+ * GPU that loads the library until the process exits; the caller still passes rho and
+ * temperature.  The entry point calls no cudaMalloc/cudaFree.  Its first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  Runs whose workspace would exceed the array return
+ * PDGPU_TOO_LARGE without touching the GPU.  All calls share the array (each run clears
+ * what it accumulates), so calls that overlap on the GPU — on different streams or host
+ * threads — race; serialise them. */
+#define PDGPU_STATIC_WORKSPACE_BYTES (32u << 20)
+pdgpu_status pdgpu_mctherm_static(int32_t nmodels, const pdgpu_model_desc* models,
+                                  const pdgpu_dust_desc* dust, const pdgpu_mc_options* options,
+                                  const float* rho, double* temperature, void* stream,
+                                  pdgpu_mc_stats* stats);
 
 /* ------------------------------------------------------------------------- */
 /* Ray-traced images and SEDs (Model.run_image, Model.run_sed)                */

@@ -60,7 +60,8 @@ class Camera(C.Structure):
 
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "time limit reached", 3: "aborted",
-          4: "packet cap", 5: "overflow", 6: "CUDA error", 7: "no device", 8: "workspace"}
+          4: "packet cap", 5: "overflow", 6: "CUDA error", 7: "no device", 8: "workspace",
+          9: "too large for the static scratch"}
 
 # Every symbol include/pdgpu.h declares (checked by the CPU test suite).
 EXPORTS = [
@@ -70,7 +71,7 @@ EXPORTS = [
     "pdgpu_mctherm", "pdgpu_mctherm_workspace_bytes", "pdgpu_mc_plan_launch_ms",
     "pdgpu_image_plan_create", "pdgpu_image_plan_destroy", "pdgpu_image_plan_info",
     "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint",
-    "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint",
+    "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint", "pdgpu_mctherm_static",
 ]
 
 
@@ -130,6 +131,9 @@ def lib(build_if_missing=True):
     L.pdgpu_image_run.argtypes = [vp, vp, vp, vp, vp, sz, vp]
     L.pdgpu_image_adjoint.restype = i32
     L.pdgpu_image_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp]
+    L.pdgpu_mctherm_static.restype = i32
+    L.pdgpu_mctherm_static.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
+                                       C.POINTER(McOptions), vp, vp, vp, C.POINTER(McStats)]
     d = C.c_double
     L.pdgpu_vis_dft.restype = i32
     L.pdgpu_vis_dft.argtypes = [i32, i32, d, d, d, d, vp, i32, vp, vp, vp, vp, vp]

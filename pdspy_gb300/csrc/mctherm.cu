@@ -986,6 +986,7 @@ const char* pdgpu_status_string(pdgpu_status s) {
         case PDGPU_CUDA_ERROR: return "CUDA error";
         case PDGPU_NO_DEVICE: return "no usable CUDA device";
         case PDGPU_WORKSPACE: return "workspace missing, too small or not uploaded";
+        case PDGPU_TOO_LARGE: return "run needs more than the library's static scratch";
         default: return "unknown status";
     }
 }
@@ -1417,3 +1418,61 @@ pdgpu_status pdgpu_mctherm(int32_t nmodels, const pdgpu_model_desc* models, cons
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Scratch-free entry point: the plan workspace lives in a file-scope device array.
+// ---------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_static_workspace[PDGPU_STATIC_WORKSPACE_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+void* g_static_address[kMaxDevices];  // device address of g_static_workspace per device
+
+// Device address of the static scratch on the current device (looked up once per device,
+// with that device current).  The host-side symbol is only a stand-in; kernels must get
+// this address.
+pdgpu_status static_workspace(void** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return PDGPU_NO_DEVICE;
+    if (dev >= kMaxDevices) return PDGPU_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_address[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_static_workspace) != cudaSuccess || !p)
+            return PDGPU_CUDA_ERROR;
+        g_static_address[dev] = p;
+    }
+    *out = g_static_address[dev];
+    return PDGPU_OK;
+}
+}  // namespace
+
+extern "C" pdgpu_status pdgpu_mctherm_static(int32_t nmodels, const pdgpu_model_desc* models,
+                                             const pdgpu_dust_desc* dust,
+                                             const pdgpu_mc_options* options, const float* rho,
+                                             double* temperature, void* stream,
+                                             pdgpu_mc_stats* stats) {
+    if (!options) return PDGPU_INVALID_ARG;
+    pdgpu_mc_options opt = *options;
+    opt.time_launches = 0;  // no event objects on this path
+    pdgpu_mc_plan* P = nullptr;
+    pdgpu_status rc = pdgpu_mc_plan_create(nmodels, models, dust, &opt, &P);
+    if (rc != PDGPU_OK) return rc;
+    if (P->ws_total > (size_t)PDGPU_STATIC_WORKSPACE_BYTES) {
+        pdgpu_mc_plan_destroy(P);
+        return PDGPU_TOO_LARGE;
+    }
+    void* ws = nullptr;
+    rc = static_workspace(&ws);
+    const size_t bytes = PDGPU_STATIC_WORKSPACE_BYTES;
+    if (rc == PDGPU_OK) rc = pdgpu_mc_plan_upload(P, ws, bytes, stream);
+    if (rc == PDGPU_OK) rc = pdgpu_mc_plan_run(P, rho, temperature, ws, bytes, stream);
+    pdgpu_mc_stats S;
+    memset(&S, 0, sizeof(S));
+    if (rc == PDGPU_OK) rc = pdgpu_mc_plan_stats(P, ws, stream, &S);
+    if (rc == PDGPU_OK && S.status != PDGPU_OK) rc = S.status;
+    if (stats) *stats = S;
+    pdgpu_mc_plan_destroy(P);
+    return rc;
+}
