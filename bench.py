@@ -120,7 +120,8 @@ def build_models(args, rank):
 
 
 def cpu_sample(models, args, threads):
-    """The CPU restatement on the first cpu-models walkers at cpu-packets packets each."""
+    """The CPU restatement on the first cpu-models walkers at cpu-packets packets each, in
+    its FP64-geometry build (native double precision is the fast choice on host cores)."""
     from oracle import orc  # noqa: F401  (CPU baseline leg only)
     from tests import _cases
     t0 = time.time()
@@ -128,7 +129,7 @@ def cpu_sample(models, args, threads):
     nm = min(args.cpu_models, len(models))
     for i, m in enumerate(models[:nm]):
         _cases.run_oracle(m, args.cpu_packets, seed=args.seed, model_id=i, nthreads=threads,
-                          **MRW)
+                          fp64_walls=True, **MRW)
         pk += args.cpu_packets
     dt = time.time() - t0
     return pk / dt, dt
@@ -153,7 +154,7 @@ def run_reference(args, world, rank):
         vals.append(v)
         times.append(dt)
     value = float(np.sum([args.cpu_models * args.cpu_packets] * args.steps) / np.sum(times))
-    sample = "%d walkers x %d packets (of the %d x %g workload), CPU restatement, %d threads" % (
+    sample = "%d walkers x %d packets (of the %d x %g workload), CPU restatement (FP64 geometry), %d threads" % (
         args.cpu_models, args.cpu_packets, args.models, args.packets, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "packets/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,

@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define PDGPU_ABI_VERSION 1
+#define PDGPU_ABI_VERSION 2
 
 typedef int32_t pdgpu_status;
 enum {
@@ -111,6 +111,9 @@ typedef struct {
     int32_t time_launches;          /* 1: record CUDA events around transport launches  */
     int64_t mrw_eager_after;        /* beyond this many events of a packet MRW is tried */
                                     /* at every event (0 = never)                       */
+    int32_t fp64_walls;             /* 0: double-single positions and wall roots (FP32  */
+                                    /* pipe, default); 1: the same kernels with FP64    */
+                                    /* geometry, the precision reference                */
 } pdgpu_mc_options;
 
 typedef struct {

@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liborc.so")
-SOURCES = ["mcrt_oracle.c", "raytrace_oracle.c"]
+SOURCES = ["mcrt_oracle.c", "geom_ds.c", "raytrace_oracle.c"]
 CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
           "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 
@@ -23,7 +23,7 @@ def needs_build():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    for f in SOURCES + ["mcrt_oracle.h", "raytrace_oracle.h"]:
+    for f in SOURCES + ["mcrt_oracle.h", "raytrace_oracle.h", "mc_internal.h"]:
         p = os.path.join(HERE, f)
         if os.path.exists(p) and os.path.getmtime(p) > t:
             return True

@@ -8,6 +8,11 @@
 
 #include "mcrt_oracle.h"
 
+/* double-single number: value = h + l, |l| <= ulp(h) / 2 */
+typedef struct {
+    float h, l;
+} ds;
+
 typedef struct {
     int nr, nt, np, ntv, mirror, ncell;
     const double* r;       /* [nr+1]            */
@@ -16,10 +21,12 @@ typedef struct {
     double* cph; double* sph; const double* ph;  /* [np+1]           */
     double* Vr; double* Vt; double* Vp;
     float* rf; float* muf; float* snf; float* cphf; float* sphf;  /* float copies */
+    float* rl; float* r2h; float* r2l; float* mu2h; float* mu2l;   /* double-single walls */
 } Geo;
 
 typedef struct {
-    double x, y, z;
+    double x, y, z;    /* position, FP64 geometry          */
+    ds sx, sy, sz;     /* position, double-single geometry */
     float kx, ky, kz;
     int ir, itv, ip;
     int lam;
@@ -42,5 +49,12 @@ void orc__free_geo(Geo* G);
 double orc__next_wall(const Geo* G, const Pkt* p, int* wall_out);
 void orc__locate_angles(const Geo* G, Pkt* p);
 int orc__cell_index(const Geo* G, const Pkt* p);
+
+/* Double-single geometry (geom_ds.c): the same walk with positions and walls in pairs of
+ * floats, evaluated operation for operation like the GPU's default geometry. */
+ds orc__next_wall_ds(const Geo* G, const Pkt* p, int* wall_out);  /* refined, as a pair */
+float orc__wall_distance_ds(const Geo* G, const Pkt* p);
+void orc__locate_angles_ds(const Geo* G, Pkt* p);
+void orc__move_ds(Pkt* p, ds s, float kx, float ky, float kz);
 
 #endif

@@ -391,12 +391,31 @@ int orc__make_geo(const orc_grid* g, Geo* G) {
     for (int i = 0; i <= g->nr; ++i) G->rf[i] = (float)g->r_edges[i];
     for (int j = 0; j <= G->ntv; ++j) { G->muf[j] = (float)G->mu[j]; G->snf[j] = (float)G->sn[j]; }
     for (int k = 0; k <= g->np; ++k) { G->cphf[k] = (float)G->cph[k]; G->sphf[k] = (float)G->sph[k]; }
+    /* double-single walls: hi = nearest float, lo = nearest float of the remainder */
+    G->rl = malloc(sizeof(float) * (g->nr + 1));
+    G->r2h = malloc(sizeof(float) * (g->nr + 1));
+    G->r2l = malloc(sizeof(float) * (g->nr + 1));
+    G->mu2h = malloc(sizeof(float) * (G->ntv + 1));
+    G->mu2l = malloc(sizeof(float) * (G->ntv + 1));
+    for (int i = 0; i <= g->nr; ++i) {
+        double R = g->r_edges[i];
+        double R2 = R * R;
+        G->rl[i] = (float)(R - (double)(float)R);
+        G->r2h[i] = (float)R2;
+        G->r2l[i] = (float)(R2 - (double)(float)R2);
+    }
+    for (int j = 0; j <= G->ntv; ++j) {
+        double m2 = G->mu[j] * G->mu[j];
+        G->mu2h[j] = (float)m2;
+        G->mu2l[j] = (float)(m2 - (double)(float)m2);
+    }
     return 0;
 }
 
 void orc__free_geo(Geo* G) {
     free(G->mu); free(G->sn); free(G->cph); free(G->sph); free(G->Vr); free(G->Vt); free(G->Vp);
     free(G->rf); free(G->muf); free(G->snf); free(G->cphf); free(G->sphf);
+    free(G->rl); free(G->r2h); free(G->r2l); free(G->mu2h); free(G->mu2l);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -719,6 +738,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
     const Tables* T = X->T;
     const orc_opts* o = X->o;
     int ns = T->nspec, nl = T->nlam;
+    const int f64 = o->fp64_walls;
     Pkt p;
     memset(&p, 0, sizeof(p));
     p.ctr[1] = pid; p.ctr[2] = (uint32_t)o->model_id; p.ctr[3] = tag;
@@ -755,22 +775,36 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         }
         int wall = W_NONE;
         double sw = 0.0;
+        /* double-single geometry: the wall distance is a pair (hi + Newton correction) and
+         * an event at the wall takes the pair; comparisons use the hi part */
+        ds swd = {0.0f, 0.0f}, sed = {sef, 0.0f};
         float tcell = 0.0f;
         int is_event = 1;
         if (full) {
-            sw = orc__next_wall(G, &p, &wall);
+            if (f64) {
+                sw = orc__next_wall(G, &p, &wall);
+            } else {
+                swd = orc__next_wall_ds(G, &p, &wall);
+                sw = (double)swd.h;
+            }
             tcell = alpha * (float)sw;
             is_event = tcell > p.tau;
             if (is_event) {
                 se = (double)(p.tau / alpha);
-                if (se > sw) se = sw;
+                sed.h = p.tau / alpha;
+                sed.l = 0.0f;
+                if (se > sw) { se = sw; sed = swd; }
             }
         }
         if (is_event) {
             /* interaction inside the cell */
-            p.x = fma(se, (double)p.kx, p.x);
-            p.y = fma(se, (double)p.ky, p.y);
-            p.z = fma(se, (double)p.kz, p.z);
+            if (f64) {
+                p.x = fma(se, (double)p.kx, p.x);
+                p.y = fma(se, (double)p.ky, p.y);
+                p.z = fma(se, (double)p.kz, p.z);
+            } else {
+                orc__move_ds(&p, sed, p.kx, p.ky, p.kz);
+            }
             p.dsafe = full ? 0.0f : p.dsafe - sef;
             p.last_wall = W_NONE;
             p.cell_events += 1;
@@ -781,7 +815,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
              * once the packet has made more than mrw_eager_after events (it is trapped). */
             if (o->mrw && (p.cell_events >= o->mrw_count_trigger ||
                            (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after))) {
-                float R0f = 0.999f * wall_distance(G, &p);
+                float R0f = 0.999f * (f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p));
                 double R0 = (double)R0f;
                 float aR = 0.0f;
                 for (int s = 0; s < ns; ++s)
@@ -816,9 +850,14 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                         dx = st * cs; dy = st * sn; dz = mu;
                     }
-                    p.x = fma(R0, (double)dx, p.x);
-                    p.y = fma(R0, (double)dy, p.y);
-                    p.z = fma(R0, (double)dz, p.z);
+                    if (f64) {
+                        p.x = fma(R0, (double)dx, p.x);
+                        p.y = fma(R0, (double)dy, p.y);
+                        p.z = fma(R0, (double)dz, p.z);
+                    } else {
+                        ds r0 = {R0f, 0.0f};
+                        orc__move_ds(&p, r0, dx, dy, dz);
+                    }
                     {
                         float mu = sqrtf(next_u(&p));
                         float sn, cs;
@@ -897,14 +936,19 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 }
                 p.tau = -orc_logf(next_u(&p));
             }
-            if (did_mrw || full) p.dsafe = 0.999999f * wall_distance(G, &p);
+            if (did_mrw || full)
+                p.dsafe = 0.999999f * (f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p));
             if (p.nevents >= o->max_interactions) { cnt->killed += 1; return p.nevents; }
             if (X->pilot && X->late_after > 0 && p.nevents >= X->late_after) return p.nevents;
         } else {
             /* move to the wall and change cell */
-            p.x = fma(sw, (double)p.kx, p.x);
-            p.y = fma(sw, (double)p.ky, p.y);
-            p.z = fma(sw, (double)p.kz, p.z);
+            if (f64) {
+                p.x = fma(sw, (double)p.kx, p.x);
+                p.y = fma(sw, (double)p.ky, p.y);
+                p.z = fma(sw, (double)p.kz, p.z);
+            } else {
+                orc__move_ds(&p, swd, p.kx, p.ky, p.kz);
+            }
             p.tau = p.tau - tcell;
             p.dsafe = 0.0f;
             p.ncross += 1;
@@ -913,7 +957,10 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             p.cell_events = 0;
             switch (wall) {
                 case W_ROUT:
-                    if (p.ir < 0) { p.ir = 0; orc__locate_angles(G, &p); }
+                    if (p.ir < 0) {
+                        p.ir = 0;
+                        if (f64) orc__locate_angles(G, &p); else orc__locate_angles_ds(G, &p);
+                    }
                     else p.ir += 1;
                     p.last_wall = W_RIN;
                     if (p.ir >= G->nr) {

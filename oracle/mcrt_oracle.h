@@ -83,6 +83,8 @@ typedef struct {
                                   /* later deposits count only at the end (0=all) */
     int64_t mrw_eager_after;      /* beyond this many events MRW is tried at      */
                                   /* every event (0 = never)                      */
+    int fp64_walls;               /* 1: FP64 positions and walls; 0: double-single */
+                                  /* (pairs of floats, the GPU's default)         */
 } orc_opts;
 
 typedef struct {

@@ -26,7 +26,7 @@ UNITS = [
     ("raytrace.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("dft.cu", []),
 ]
-HEADERS = ["mc_common.h", "mc_device.cuh", "mc_geom.cuh", "mc_host.h"]
+HEADERS = ["mc_common.h", "mc_device.cuh", "mc_geom.cuh", "mc_geom_ds.cuh", "mc_host.h"]
 
 
 def nvcc():

@@ -32,7 +32,7 @@ class McOptions(C.Structure):
                 ("deadline_ns", C.c_int64), ("abort_flag", C.c_void_p),
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("late_after", C.c_int64), ("time_launches", C.c_int32),
-                ("mrw_eager_after", C.c_int64)]
+                ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int32)]
 
 
 class McStats(C.Structure):

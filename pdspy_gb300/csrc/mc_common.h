@@ -41,6 +41,7 @@ struct McModel {
     int32_t off_r, off_mu, off_sn, off_cph, off_sph, off_vr, off_vt, off_vp;  // dpool
     int32_t off_star;            // fpool offset of the stellar CDF [nlam]
     int32_t off_rf, off_muf, off_snf, off_cphf, off_sphf;  // fpool: float wall copies
+    int32_t off_rl, off_r2h, off_r2l, off_mu2h, off_mu2l;  // fpool: double-single walls
     int32_t model_id;
     double q_unit;               // erg/s per fixed-point unit
     double lum;                  // erg/s

@@ -85,6 +85,30 @@ inline bool append_geometry(int nr, int nt, int np, const double* r_edges,
     for (int k = 0; k <= np; ++k) fp.push_back((float)dp[M.off_cph + k]);
     M.off_sphf = (int)fp.size();
     for (int k = 0; k <= np; ++k) fp.push_back((float)dp[M.off_sph + k]);
+    // double-single walls: hi = nearest float, lo = nearest float of the remainder
+    auto lo_part = [](double v) { return (float)(v - (double)(float)v); };
+    M.off_rl = (int)fp.size();
+    for (int i = 0; i <= nr; ++i) fp.push_back(lo_part(dp[M.off_r + i]));
+    M.off_r2h = (int)fp.size();
+    for (int i = 0; i <= nr; ++i) {
+        double R = dp[M.off_r + i];
+        fp.push_back((float)(R * R));
+    }
+    M.off_r2l = (int)fp.size();
+    for (int i = 0; i <= nr; ++i) {
+        double R = dp[M.off_r + i];
+        fp.push_back(lo_part(R * R));
+    }
+    M.off_mu2h = (int)fp.size();
+    for (int j = 0; j <= M.ntv; ++j) {
+        double mu = dp[M.off_mu + j];
+        fp.push_back((float)(mu * mu));
+    }
+    M.off_mu2l = (int)fp.size();
+    for (int j = 0; j <= M.ntv; ++j) {
+        double mu = dp[M.off_mu + j];
+        fp.push_back(lo_part(mu * mu));
+    }
     while (fp.size() % 4) fp.push_back(0.0f);
     return true;
 }

@@ -21,8 +21,14 @@
 // q' = q_lo + u * q_span (energy absorbed per gram per second), with q_lo from the
 // energy absorbed in earlier epochs and q_span = q_lo (b_{k+1}/b_k - 1) its expected
 // growth over the epoch.  The first epoch runs npilot pilot passes that estimate its own
-// span.  FP64 is used for the wall-intersection root solves (and the packet position
-// they update) and for the energy -> temperature inversion; everything else is FP32.
+// span.
+//
+// Precision.  Radiative quantities (optical depths, opacities, random numbers, reemission
+// sampling) are FP32.  The packet position, the safety distance and the wall-intersection
+// roots use double-single arithmetic on the FP32 pipe (mc_geom_ds.cuh explains why FP64 is
+// not used for them on GB300); the same kernels instantiated with FP64 geometry
+// (mc_geom.cuh) are selected by pdgpu_mc_options.fp64_walls and serve as the precision
+// reference.  The energy -> temperature inversion is FP64 (once per cell).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,15 +44,16 @@
 #include "mc_common.h"
 #include "mc_device.cuh"
 #include "mc_geom.cuh"
+#include "mc_geom_ds.cuh"
 #include "mc_host.h"
 
 namespace {
 using namespace pdgpu;
 
-// Saved state of a parked packet (everything in Pkt except the Philox buffer, which is
-// regenerated from the draw counter).
+// Saved state of a parked packet (everything in the packet except the Philox buffer, which
+// is regenerated from the draw counter).  pos holds the position bits of either geometry.
 struct __align__(16) ParkRec {
-    double x, y, z;
+    uint64_t pos[3];
     float dsafe, kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events, nevents, ncross;
@@ -106,6 +113,140 @@ struct Cnt {
     int maxev;
 };
 
+// Geometry policies of the transport step.
+//
+// GeoS: double-single positions and walls (mc_geom_ds.cuh), the default.
+// GeoD: the same walk with FP64 positions and walls (mc_geom.cuh), the precision reference.
+// Each provides the packet type, the length type of a move, and the wall operations for a
+// packet per thread (wall_lane) or per warp (wall_warp: candidate k on lane k, reduced with
+// the serial tie-break, first candidate with the smallest distance).
+struct GeoS {
+    using Pkt = PktS;
+    using len_t = ds;   // wall distances keep the Newton correction as the lo part
+    static __device__ __forceinline__ ds of(float v) { return ds{v, 0.0f}; }
+    static __device__ __forceinline__ float f(ds v) { return v.h; }
+    static __device__ __forceinline__ bool gt(ds a, ds b) { return a.h > b.h; }
+    static __device__ __forceinline__ int cell(const McModel& M, const Pkt& p) { return cell_of_s(M, p); }
+    static __device__ __forceinline__ ds wall_lane(const McModel& M, const double*, const float* fp,
+                                                   const Pkt& p, int& w) {
+        WallsS W(M, fp);
+        return next_wall_ds(M, W, p, w);
+    }
+    static __device__ __forceinline__ ds wall_warp(int lane, const McModel& M, const double*,
+                                                   const float* fp, const Pkt& p, int& w) {
+        WallsS W(M, fp);
+        FrameS f;
+        frame_ds(M, W, p, f);
+        const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
+        float s = 3.0e38f;
+        int k = 64 + lane;
+        if (lane < nk) {
+            float v;
+            if (candidate_ds(M, W, p, f, lane, v)) { s = v; k = lane; }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            float so = __shfl_xor_sync(0xffffffffu, s, o);
+            int ko = __shfl_xor_sync(0xffffffffu, k, o);
+            if (so < s || (so == s && ko < k)) { s = so; k = ko; }
+        }
+        s = __shfl_sync(0xffffffffu, s, 0);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= 64) { w = W_NONE; return ds{3.0e38f, 0.0f}; }
+        w = cand_wall_code(k);
+        return refine_ds(M, W, p, f, k, s);
+    }
+    static __device__ __forceinline__ float dist(const McModel& M, const double*, const float* fp,
+                                                 const Pkt& p) {
+        WallsS W(M, fp);
+        return wall_distance_ds(M, W, p);
+    }
+    static __device__ __forceinline__ void locate(const McModel& M, const double*, const float* fp,
+                                                  Pkt& p) {
+        WallsS W(M, fp);
+        locate_angles_ds(M, W, p);
+    }
+    static __device__ __forceinline__ void move(Pkt& p, ds s, float kx, float ky, float kz) {
+        p.x = ds_move2(p.x, s, kx);
+        p.y = ds_move2(p.y, s, ky);
+        p.z = ds_move2(p.z, s, kz);
+    }
+    static __device__ __forceinline__ void origin(Pkt& p) {
+        p.x = ds{0.0f, 0.0f}; p.y = ds{0.0f, 0.0f}; p.z = ds{0.0f, 0.0f};
+    }
+    static __device__ __forceinline__ uint64_t pack(ds v) {
+        return (uint64_t)__float_as_uint(v.h) | ((uint64_t)__float_as_uint(v.l) << 32);
+    }
+    static __device__ __forceinline__ ds unpack(uint64_t b) {
+        return ds{__uint_as_float((uint32_t)b), __uint_as_float((uint32_t)(b >> 32))};
+    }
+    static __device__ __forceinline__ void save(ParkRec& r, const Pkt& p) {
+        r.pos[0] = pack(p.x); r.pos[1] = pack(p.y); r.pos[2] = pack(p.z);
+    }
+    static __device__ __forceinline__ void load(Pkt& p, const ParkRec& r) {
+        p.x = unpack(r.pos[0]); p.y = unpack(r.pos[1]); p.z = unpack(r.pos[2]);
+    }
+};
+
+struct GeoD {
+    using Pkt = pdgpu::Pkt;
+    using len_t = double;
+    static __device__ __forceinline__ double of(float v) { return (double)v; }
+    static __device__ __forceinline__ float f(double v) { return (float)v; }
+    static __device__ __forceinline__ bool gt(double a, double b) { return a > b; }
+    static __device__ __forceinline__ int cell(const McModel& M, const Pkt& p) { return cell_of(M, p); }
+    static __device__ __forceinline__ double wall_lane(const McModel& M, const double* dp, const float*,
+                                                       const Pkt& p, int& w) {
+        return next_wall(M, dp, p, w);
+    }
+    static __device__ __forceinline__ double wall_warp(int lane, const McModel& M, const double* dp,
+                                                       const float*, const Pkt& p, int& w) {
+        WallFrame f;
+        wall_frame(M, dp, p, f);
+        const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
+        double s = 1.0e300;
+        int k = 64 + lane;
+        if (lane < nk) {
+            double v;
+            if (wall_candidate(M, dp, p, f, lane, v)) { s = v; k = lane; }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            double so = __shfl_xor_sync(0xffffffffu, s, o);
+            int ko = __shfl_xor_sync(0xffffffffu, k, o);
+            if (so < s || (so == s && ko < k)) { s = so; k = ko; }
+        }
+        s = __shfl_sync(0xffffffffu, s, 0);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        w = (k < 64) ? wall_code(k) : W_NONE;
+        return (k < 64) ? s : 1.0e300;
+    }
+    static __device__ __forceinline__ float dist(const McModel& M, const double* dp, const float* fp,
+                                                 const Pkt& p) {
+        return wall_distance(M, dp, fp, p);
+    }
+    static __device__ __forceinline__ void locate(const McModel& M, const double* dp, const float*,
+                                                  Pkt& p) {
+        locate_angles(M, dp, p);
+    }
+    static __device__ __forceinline__ void move(Pkt& p, double s, float kx, float ky, float kz) {
+        p.x = fma(s, (double)kx, p.x);
+        p.y = fma(s, (double)ky, p.y);
+        p.z = fma(s, (double)kz, p.z);
+    }
+    static __device__ __forceinline__ void origin(Pkt& p) { p.x = 0.0; p.y = 0.0; p.z = 0.0; }
+    static __device__ __forceinline__ void save(ParkRec& r, const Pkt& p) {
+        r.pos[0] = (uint64_t)__double_as_longlong(p.x);
+        r.pos[1] = (uint64_t)__double_as_longlong(p.y);
+        r.pos[2] = (uint64_t)__double_as_longlong(p.z);
+    }
+    static __device__ __forceinline__ void load(Pkt& p, const ParkRec& r) {
+        p.x = __longlong_as_double((long long)r.pos[0]);
+        p.y = __longlong_as_double((long long)r.pos[1]);
+        p.z = __longlong_as_double((long long)r.pos[2]);
+    }
+};
+
 // Execution policies of the transport step.
 //
 // LanePol: one packet per thread (the epoch launches).
@@ -113,9 +254,8 @@ struct Cnt {
 // long parked packets, whose sequential chains set the run time).  The lanes share the
 // work that is independent within a step: a window of 32 Philox blocks is generated at
 // once (lane i holds block base+i, a draw is a shuffle), table searches count the entries
-// <= the key with ballots, and the six wall candidates are solved by lanes 0..5 and reduced
-// with the serial tie-break (first candidate with the smallest distance).  Every result is
-// identical to the per-thread code; memory side effects are issued by lane 0 only.
+// <= the key with ballots, and the wall candidates are solved on separate lanes.  Every
+// result is identical to the per-thread code; memory side effects are issued by lane 0.
 struct LanePol {
     __device__ __forceinline__ float next(McRng& r, uint32_t k0, uint32_t k1) {
         return mc_next(r, k0, k1);
@@ -126,9 +266,11 @@ struct LanePol {
     __device__ __forceinline__ void row(const float* F, float q, int& j, float& w) const {
         mc_row_search(F, q, j, w);
     }
-    __device__ __forceinline__ double wall(const McModel& M, const double* dp, const Pkt& p,
-                                           int& w) const {
-        return next_wall(M, dp, p, w);
+    template <class G>
+    __device__ __forceinline__ typename G::len_t wall(const McModel& M, const double* dp,
+                                                      const float* fp, const typename G::Pkt& p,
+                                                      int& w) const {
+        return G::wall_lane(M, dp, fp, p, w);
     }
     __device__ __forceinline__ bool leader() const { return true; }
 };
@@ -179,30 +321,11 @@ struct WarpPol {
             if (w > 1.0f) w = 1.0f;
         }
     }
-    __device__ __forceinline__ double wall(const McModel& M, const double* dp, const Pkt& p,
-                                           int& w) const {
-        WallFrame f;
-        wall_frame(M, dp, p, f);
-        const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
-        double s = 1.0e300;
-        int k = lane;
-        if (lane < nk) {
-            double v;
-            if (!wall_candidate(M, dp, p, f, lane, v)) k = 64 + lane;
-            else s = v;
-        } else {
-            k = 64 + lane;
-        }
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) {
-            double so = __shfl_xor_sync(0xffffffffu, s, o);
-            int ko = __shfl_xor_sync(0xffffffffu, k, o);
-            if (so < s || (so == s && ko < k)) { s = so; k = ko; }
-        }
-        s = __shfl_sync(0xffffffffu, s, 0);
-        k = __shfl_sync(0xffffffffu, k, 0);
-        w = (k < 64) ? wall_code(k) : W_NONE;
-        return (k < 64) ? s : 1.0e300;
+    template <class G>
+    __device__ __forceinline__ typename G::len_t wall(const McModel& M, const double* dp,
+                                                      const float* fp, const typename G::Pkt& p,
+                                                      int& w) const {
+        return G::wall_warp(lane, M, dp, fp, p, w);
     }
     __device__ __forceinline__ bool leader() const { return lane == 0; }
 };
@@ -217,19 +340,20 @@ __device__ __forceinline__ float row_interp(Pol& pol, const DustTabs& T, const f
 }
 
 template <class Pol>
-__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, Pkt& p,
+__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, McRng& rng,
                                              uint32_t k0, uint32_t k1, float2 q, int s) {
-    float uq = pol.next(p.rng, k0, k1);
+    float uq = pol.next(rng, k0, k1);
     float qq = q.x + uq * q.y;
     int j;
     float w;
     pol.row(T.F + s * MC_NROW, qq, j, w);
-    int row = j + ((pol.next(p.rng, k0, k1) < w) ? 1 : 0);
-    return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, pol.next(p.rng, k0, k1));
+    int row = j + ((pol.next(rng, k0, k1) < w) ? 1 : 0);
+    return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, pol.next(rng, k0, k1));
 }
 
-__device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* star_cdf, int nl,
-                                     uint32_t k0, uint32_t k1) {
+template <class G>
+__device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, const float* star_cdf,
+                                     int nl, uint32_t k0, uint32_t k1) {
     float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
     float sn, cs;
     mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
@@ -239,7 +363,7 @@ __device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* sta
     p.kz = mu;
     p.lam = mc_cdf_search(star_cdf, nl, mc_next(p.rng, k0, k1));
     p.tau = -mc_logf(mc_next(p.rng, k0, k1));
-    p.x = 0.0; p.y = 0.0; p.z = 0.0;
+    G::origin(p);
     p.dsafe = 0.0f;
     p.ir = -1; p.itv = 0; p.ip = 0;
     p.last_wall = W_NONE;
@@ -250,8 +374,9 @@ __device__ __forceinline__ void emit(Pkt& p, const DustTabs& T, const float* sta
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
 // has left the grid or was killed.
-template <int NS, class Pol>
-__device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, Pol& pol) {
+template <int NS, class Pol, class G>
+__device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, Pol& pol) {
+    using len_t = typename G::len_t;
     const McModel& M = P.models[p.m];
     const double* __restrict__ dp = P.dpool;
     const int nl = P.nl;
@@ -261,7 +386,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
     float rh[NS];
     const int64_t base = M.cell_off;
     if (p.ir >= 0) {
-        c = cell_of(M, p);
+        c = G::cell(M, p);
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             rh[s] = __ldg(P.rho + base + (int64_t)s * M.ncell + c);
@@ -271,29 +396,27 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
     // Safety distance: an interaction closer than the isotropic distance to the nearest
     // wall needs no wall solve (the common case in optically thick cells).
     bool full = true;
-    double se = 0.0;
+    len_t se = G::of(0.0f);
     float sef = 0.0f;
     if (alpha > 0.0f) {
         sef = p.tau / alpha;
-        if (sef < p.dsafe) { full = false; se = (double)sef; }
+        if (sef < p.dsafe) { full = false; se = G::of(sef); }
     }
     int wall = W_NONE;
-    double sw = 0.0;
+    len_t sw = G::of(0.0f);
     float tcell = 0.0f;
     bool is_event = true;
     if (full) {
-        sw = pol.wall(M, dp, p, wall);
-        tcell = alpha * (float)sw;
+        sw = pol.template wall<G>(M, dp, P.fpool, p, wall);
+        tcell = alpha * G::f(sw);
         is_event = tcell > p.tau;
         if (is_event) {
-            se = (double)(p.tau / alpha);
-            if (se > sw) se = sw;
+            se = G::of(p.tau / alpha);
+            if (G::gt(se, sw)) se = sw;
         }
     }
     if (is_event) {
-        p.x = fma(se, (double)p.kx, p.x);
-        p.y = fma(se, (double)p.ky, p.y);
-        p.z = fma(se, (double)p.kz, p.z);
+        G::move(p, se, p.kx, p.ky, p.kz);
         p.dsafe = full ? 0.0f : p.dsafe - sef;
         p.last_wall = W_NONE;
         p.cell_events += 1;
@@ -307,8 +430,8 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
         // the packet has made more than mrw_eager_after events (it is trapped).
         if (P.mrw && (p.cell_events >= P.mrw_trigger ||
                       (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after))) {
-            float R0f = 0.999f * wall_distance(M, dp, P.fpool, p);
-            double R0 = (double)R0f;
+            float R0f = 0.999f * G::dist(M, dp, P.fpool, p);
+            len_t R0 = G::of(R0f);
             float2 qv[NS];
             float aR = 0.0f;
 #pragma unroll
@@ -346,9 +469,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     dx = st * cs; dy = st * sn; dz = mu;
                 }
-                p.x = fma(R0, (double)dx, p.x);
-                p.y = fma(R0, (double)dy, p.y);
-                p.z = fma(R0, (double)dz, p.z);
+                G::move(p, R0, dx, dy, dz);
                 {
                     float mu = sqrtf(pol.next(p.rng, k0, k1));
                     float sn, cs;
@@ -372,7 +493,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
 #pragma unroll
                 for (int s = 1; s < NS; ++s)
                     if (s == sp) qs = qv[s];
-                p.lam = reemit_lambda(pol, T, nl, p, k0, k1, qs, sp);
+                p.lam = reemit_lambda(pol, T, nl, p.rng, k0, k1, qs, sp);
                 p.tau = -mc_logf(pol.next(p.rng, k0, k1));
                 p.cell_events = 0;
                 cnt.mrw += 1;
@@ -427,7 +548,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
-                p.lam = reemit_lambda(pol, T, nl, p, k0, k1, qa[idx], sp);
+                p.lam = reemit_lambda(pol, T, nl, p.rng, k0, k1, qa[idx], sp);
                 {
                     float mu = 2.0f * pol.next(p.rng, k0, k1) - 1.0f;
                     float sn, cs;
@@ -439,7 +560,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
             }
             p.tau = -mc_logf(pol.next(p.rng, k0, k1));
         }
-        if (did_mrw || full) p.dsafe = 0.999999f * wall_distance(M, dp, P.fpool, p);
+        if (did_mrw || full) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
         if (late) cnt.late += 1;
         if (p.nevents >= P.max_inter) {
             cnt.killed += 1;
@@ -450,7 +571,8 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
             unsigned long long slot = atomicAdd(P.park_count, 1ull);
             if ((long long)slot < P.park_cap) {
                 ParkRec r;
-                r.x = p.x; r.y = p.y; r.z = p.z; r.dsafe = p.dsafe;
+                G::save(r, p);
+                r.dsafe = p.dsafe;
                 r.kx = p.kx; r.ky = p.ky; r.kz = p.kz; r.tau = p.tau;
                 r.ir = p.ir; r.itv = p.itv; r.ip = p.ip; r.lam = p.lam;
                 r.last_wall = p.last_wall; r.cell_events = p.cell_events;
@@ -464,9 +586,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
         }
         return true;
     }
-    p.x = fma(sw, (double)p.kx, p.x);
-    p.y = fma(sw, (double)p.ky, p.y);
-    p.z = fma(sw, (double)p.kz, p.z);
+    G::move(p, sw, p.kx, p.ky, p.kz);
     p.tau = p.tau - tcell;
     p.dsafe = 0.0f;
     p.ncross += 1;
@@ -474,7 +594,7 @@ __device__ bool mc_step(Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, 
     p.cell_events = 0;
     switch (wall) {
         case W_ROUT:
-            if (p.ir < 0) { p.ir = 0; locate_angles(M, dp, p); }
+            if (p.ir < 0) { p.ir = 0; G::locate(M, dp, P.fpool, p); }
             else p.ir += 1;
             p.last_wall = W_RIN;
             if (p.ir >= M.nr) {
@@ -509,7 +629,7 @@ __device__ __forceinline__ unsigned long long globaltimer() {
     return t;
 }
 
-template <int NS>
+template <int NS, class G>
 __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
@@ -544,7 +664,7 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    Pkt p;
+    typename G::Pkt p;
     bool active = false;
     unsigned iter = 0;
     LanePol lanepol;
@@ -571,14 +691,14 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
                     p.rng.model = (uint32_t)M.model_id;
                     p.rng.tag = P.tag;
                     p.rng.draw = 0;
-                    emit(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
+                    emit<G>(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
                     active = true;
                 }
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
-            active = mc_step<NS>(p, P, T, cnt, lanepol);
+            active = mc_step<NS, LanePol, G>(p, P, T, cnt, lanepol);
             if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
         }
         if (((++iter) & 4095u) == 0u) {
@@ -626,7 +746,7 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
 }
 
 // Continuation of parked packets: one packet per warp (WarpPol), taken from a queue.
-template <int NS>
+template <int NS, class G>
 __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
@@ -661,8 +781,9 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         g = __shfl_sync(0xffffffffu, g, 0);
         if ((long long)g >= total) break;
         const ParkRec r = P.park[g];
-        Pkt p;
-        p.x = r.x; p.y = r.y; p.z = r.z; p.dsafe = r.dsafe;
+        typename G::Pkt p;
+        G::load(p, r);
+        p.dsafe = r.dsafe;
         p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
         p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
         p.last_wall = r.last_wall; p.cell_events = r.cell_events;
@@ -671,7 +792,7 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         WarpPol pol(lane);
         bool alive = true;
         while (alive) {
-            alive = mc_step<NS>(p, P, T, cnt, pol);
+            alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
                 if (lane == 0) {
@@ -1251,19 +1372,20 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.count_stats = final_pass ? 1 : 0;
     if (prm.total <= 0) return PDGPU_OK;
     void (*kern)(McParams) = nullptr;
+    const bool f64 = P->opt.fp64_walls != 0;
     if (phase == 0) {
         switch (P->ns) {
-            case 1: kern = mc_transport_kernel<1>; break;
-            case 2: kern = mc_transport_kernel<2>; break;
-            case 3: kern = mc_transport_kernel<3>; break;
-            default: kern = mc_transport_kernel<4>; break;
+            case 1: kern = f64 ? mc_transport_kernel<1, GeoD> : mc_transport_kernel<1, GeoS>; break;
+            case 2: kern = f64 ? mc_transport_kernel<2, GeoD> : mc_transport_kernel<2, GeoS>; break;
+            case 3: kern = f64 ? mc_transport_kernel<3, GeoD> : mc_transport_kernel<3, GeoS>; break;
+            default: kern = f64 ? mc_transport_kernel<4, GeoD> : mc_transport_kernel<4, GeoS>; break;
         }
     } else {
         switch (P->ns) {
-            case 1: kern = mc_continue_kernel<1>; break;
-            case 2: kern = mc_continue_kernel<2>; break;
-            case 3: kern = mc_continue_kernel<3>; break;
-            default: kern = mc_continue_kernel<4>; break;
+            case 1: kern = f64 ? mc_continue_kernel<1, GeoD> : mc_continue_kernel<1, GeoS>; break;
+            case 2: kern = f64 ? mc_continue_kernel<2, GeoD> : mc_continue_kernel<2, GeoS>; break;
+            case 3: kern = f64 ? mc_continue_kernel<3, GeoD> : mc_continue_kernel<3, GeoS>; break;
+            default: kern = f64 ? mc_continue_kernel<4, GeoD> : mc_continue_kernel<4, GeoS>; break;
         }
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem_bytes) !=

@@ -27,5 +27,5 @@ def test_library_exports_declared_symbols():
 
 def test_abi_version_and_status_strings():
     L = _lib.lib()
-    assert L.pdgpu_abi_version() == 1
+    assert L.pdgpu_abi_version() == 2
     assert L.pdgpu_status_string(2) == b"time limit reached"

@@ -43,6 +43,20 @@ def test_plain_bit_exact(cuda, name):
         assert st["parked"] > 0 and st["late_units"] > 0
 
 
+@pytest.mark.parametrize("name", ["disk_full", "two_species_mrw", "spiral_3d", "parked"])
+def test_fp64_geometry_bit_exact(cuda, name):
+    """The precision-reference instantiation (FP64 positions and walls) against the
+    oracle's FP64 geometry."""
+    m, kw = _cases.case(name)
+    nphot = 3000
+    plan, E, T, st = _gpu_run([m], nphot, seed=5, fp64_walls=True, **kw)
+    ref = _cases.run_oracle(m, nphot, seed=5, fp64_walls=True, **kw)
+    assert np.array_equal(E, ref["energy"].reshape(-1)), name
+    assert np.array_equal(T, ref["temperature"].reshape(-1)), name
+    for k in ("escaped", "killed", "crossings", "events", "mrw_steps"):
+        assert st[k] == ref["stats"][k], (name, k)
+
+
 def test_batched_matches_each_model(cuda):
     models = workloads.walker_models(n=3, seed=5, scale=0.15)
     nphot = [3000, 1500, 4500]

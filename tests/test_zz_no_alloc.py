@@ -38,7 +38,9 @@ def _descriptors(models, nphot, keep):
         ka.append(a); ks.append(s); gg.append(np.zeros_like(a) if gv is None else gv)
     dust = _lib.DustDesc(len(g.lam), len(g.dust), arr(g.lam), arr(np.stack(ka)),
                          arr(np.stack(ks)), arr(np.stack(gg)))
-    opts = _lib.McOptions(5, 8, 2, 1, 2.0, 10.0, 20, 2_000_000_000, 0, None, 0, 0, 200, 0, 200)
+    opts = _lib.McOptions(seed=5, nepoch=8, npilot=2, mrw=1, mrw_gamma=2.0, mrw_tauthres=10.0,
+                          mrw_count_trigger=20, max_interactions=2_000_000_000, late_after=200,
+                          mrw_eager_after=200)
     return descs, dust, opts
 
 
