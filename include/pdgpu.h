@@ -114,6 +114,12 @@ typedef struct {
     int32_t fp64_walls;             /* 0: double-single positions and wall roots (FP32  */
                                     /* pipe, default); 1: the same kernels with FP64    */
                                     /* geometry, the precision reference                */
+    int32_t no_batch;               /* 1: continue long packets one interaction at a    */
+                                    /* time instead of in speculative warp batches      */
+                                    /* (identical results; for timing comparisons)      */
+    int64_t drain_below;            /* resumed packets run one per thread until fewer   */
+                                    /* than this many are left, then one per warp       */
+                                    /* (0 = the warp launch's width, -1 = never)        */
 } pdgpu_mc_options;
 
 typedef struct {
@@ -121,8 +127,9 @@ typedef struct {
         mrw_steps;
     int32_t status;                 /* pdgpu_status reached by the device               */
     int32_t launches;               /* transport launches of the last run               */
-    int64_t parked;                 /* packets resumed by the continuation launch       */
-    int64_t late_units;             /* energy deposited after late_after events         */
+    int64_t parked;                 /* packets resumed by the continuation launches     */
+    int64_t late_units;             /* interactions after a packet's late_after-th      */
+    int64_t drained;                /* resumed packets finished one per warp            */
 } pdgpu_mc_stats;
 
 /* Byte offsets of the run's device arrays inside the workspace. */

@@ -422,14 +422,17 @@ void orc__free_geo(Geo* G) {
 /* Packet                                                                     */
 /* ------------------------------------------------------------------------- */
 
-static inline float next_u(Pkt* p) {
-    uint32_t i = p->draw & 3u;
-    if (i == 0u) {
-        p->ctr[0] = p->draw >> 2;
-        orc_philox4x32_10(p->ctr, p->key, p->buf);
-    }
-    p->draw += 1u;
-    return u01(p->buf[i]);
+/* Random numbers of interaction n of a packet: one Philox block per stream with counter
+ * (n, packet id, model, pass tag | stream << 24).  Streams: 0 albedo test, new optical
+ * depth, direction cosine, azimuth; 1 reemission q', reemission row, reemission CDF,
+ * species; 2 MRW diffusion time, jump cosine, jump azimuth; 3 (n = 0) the emission. */
+enum { RS_EVENT = 0, RS_SECOND = 1, RS_MRW = 2, RS_EMIT = 3 };
+
+static inline void ev_block(const Pkt* p, uint32_t n, uint32_t stream, float u[4]) {
+    uint32_t c[4], o[4];
+    c[0] = n; c[1] = p->ctr[1]; c[2] = p->ctr[2]; c[3] = p->ctr[3] | (stream << 24);
+    orc_philox4x32_10(c, p->key, o);
+    for (int i = 0; i < 4; ++i) u[i] = u01(o[i]);
 }
 
 
@@ -588,10 +591,10 @@ static void rotate_dir(float* kx, float* ky, float* kz, float mu, float cp, floa
     *kx = nx / n; *ky = ny / n; *kz = nz / n;
 }
 
-static void iso_dir(Pkt* p) {
-    float mu = 2.0f * next_u(p) - 1.0f;
+static void iso_dir(Pkt* p, float umu, float uphi) {
+    float mu = 2.0f * umu - 1.0f;
     float sn, cs;
-    orc_sincospif2(next_u(p), &sn, &cs);
+    orc_sincospif2(uphi, &sn, &cs);
     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
     p->kx = st * cs; p->ky = st * sn; p->kz = mu;
 }
@@ -651,10 +654,10 @@ static void atomic_add64(int64_t* a, int64_t v) { __atomic_fetch_add(a, v, __ATO
 #define DEP(X, p) (((X)->late_after > 0 && (p).nevents > (X)->late_after) ? (X)->Elate : (X)->E)
 
 /* Reemission wavelength for species s in cell c. */
-static int reemit_lambda(const Ctx* X, Pkt* p, int s, int c) {
+/* Reemission wavelength bin of species s in cell c from the uniforms (uq, urow, ucdf). */
+static int reemit_lambda(const Ctx* X, int s, int c, float uq, float urow, float ucdf) {
     const Tables* T = X->T;
     size_t sc = (size_t)s * X->G->ncell + c;
-    float uq = next_u(p);
     float q;
     if (X->sequential) {
         int64_t e = __atomic_load_n(&X->E[sc], __ATOMIC_RELAXED);
@@ -665,8 +668,8 @@ static int reemit_lambda(const Ctx* X, Pkt* p, int s, int c) {
     int j;
     float w;
     row_search(T->Ff + (size_t)s * ORC_NROW, q, &j, &w);
-    int row = j + ((next_u(p) < w) ? 1 : 0);
-    return cdf_search(T->cdf + ((size_t)s * ORC_NROW + row) * T->nlam, T->nlam, next_u(p));
+    int row = j + ((urow < w) ? 1 : 0);
+    return cdf_search(T->cdf + ((size_t)s * ORC_NROW + row) * T->nlam, T->nlam, ucdf);
 }
 
 /* Frozen-row interpolation of a [NROW] table at the cell's mid-epoch energy. */
@@ -746,13 +749,15 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
     p.key[1] = (uint32_t)(o->seed >> 32);
     /* emission */
     {
-        float mu = 2.0f * next_u(&p) - 1.0f;
+        float e[4];
+        ev_block(&p, 0u, RS_EMIT, e);
+        float mu = 2.0f * e[0] - 1.0f;
         float sn, cs;
-        orc_sincospif2(next_u(&p), &sn, &cs);
+        orc_sincospif2(e[1], &sn, &cs);
         float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
         p.kx = st * cs; p.ky = st * sn; p.kz = mu;
-        p.lam = cdf_search(T->star_cdf, nl, next_u(&p));
-        p.tau = -orc_logf(next_u(&p));
+        p.lam = cdf_search(T->star_cdf, nl, e[2]);
+        p.tau = -orc_logf(e[3]);
         p.ir = -1; p.itv = 0; p.ip = 0;
         p.last_wall = W_NONE;
     }
@@ -807,15 +812,22 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             }
             p.dsafe = full ? 0.0f : p.dsafe - sef;
             p.last_wall = W_NONE;
+            const uint32_t n = (uint32_t)p.nevents;   /* index of this interaction */
             p.cell_events += 1;
             p.nevents += 1;
             cnt->events += 1;
+            float ev[4], sb[4];
+            ev_block(&p, n, RS_EVENT, ev);
             int did_mrw = 0;
             /* MRW is tried after mrw_count_trigger events in one cell, and at every event
-             * once the packet has made more than mrw_eager_after events (it is trapped). */
-            if (o->mrw && (p.cell_events >= o->mrw_count_trigger ||
-                           (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after))) {
-                float R0f = 0.999f * (f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p));
+             * once the packet has made more than mrw_eager_after events (it is trapped).
+             * The wall distance of a try also refreshes the safety distance. */
+            const int tried = o->mrw && (p.cell_events >= o->mrw_count_trigger ||
+                                         (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after));
+            float Dw = 0.0f;
+            if (tried) {
+                Dw = f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p);
+                float R0f = 0.999f * Dw;
                 double R0 = (double)R0f;
                 float aR = 0.0f;
                 for (int s = 0; s < ns; ++s)
@@ -823,7 +835,10 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                                   row_interp(X, T->kR + (size_t)s * ORC_NROW, s, c);
                 if (R0f * aR >= o->mrw_gamma && R0f * alpha >= o->mrw_tauthres) {
                     did_mrw = 1;
-                    float uy = next_u(&p);
+                    float mb[4];
+                    ev_block(&p, n, RS_MRW, mb);
+                    ev_block(&p, n, RS_SECOND, sb);
+                    float uy = mb[0];
                     float f = uy * (float)(ORC_NMRW - 1);
                     int i = (int)f;
                     if (i > ORC_NMRW - 2) i = ORC_NMRW - 2;
@@ -844,9 +859,9 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                     /* jump to the sphere surface */
                     float dx, dy, dz;
                     {
-                        float mu = 2.0f * next_u(&p) - 1.0f;
+                        float mu = 2.0f * mb[1] - 1.0f;
                         float sn, cs;
-                        orc_sincospif2(next_u(&p), &sn, &cs);
+                        orc_sincospif2(mb[2], &sn, &cs);
                         float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                         dx = st * cs; dy = st * sn; dz = mu;
                     }
@@ -859,16 +874,16 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         orc__move_ds(&p, r0, dx, dy, dz);
                     }
                     {
-                        float mu = sqrtf(next_u(&p));
+                        float mu = sqrtf(ev[2]);
                         float sn, cs;
-                        orc_sincospif2(next_u(&p), &sn, &cs);
+                        orc_sincospif2(ev[3], &sn, &cs);
                         float kx = dx, ky = dy, kz = dz;
                         rotate_dir(&kx, &ky, &kz, mu, cs, sn);
                         p.kx = kx; p.ky = ky; p.kz = kz;
                     }
                     int sp = 0;
                     if (ns > 1) {
-                        float us = next_u(&p) * aP;
+                        float us = sb[3] * aP;
                         float acc = 0.0f;
                         sp = ns - 1;
                         for (int s = 0; s < ns; ++s) {
@@ -876,14 +891,14 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                             if (us < acc) { sp = s; break; }
                         }
                     }
-                    p.lam = reemit_lambda(X, &p, sp, c);
-                    p.tau = -orc_logf(next_u(&p));
+                    p.lam = reemit_lambda(X, sp, c, sb[0], sb[1], sb[2]);
+                    p.tau = -orc_logf(ev[1]);
                     p.cell_events = 0;
                     cnt->mrw += 1;
                 }
             }
             if (!did_mrw) {
-                float ua = next_u(&p);
+                float ua = ev[0];
                 float asca = 0.0f;
                 for (int s = 0; s < ns; ++s)
                     asca = asca + X->rho[(size_t)s * G->ncell + c] * T->ksca[(size_t)s * nl + p.lam];
@@ -891,7 +906,8 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                     /* scattering */
                     int sp = 0;
                     if (ns > 1) {
-                        float us = next_u(&p) * asca;
+                        ev_block(&p, n, RS_SECOND, sb);
+                        float us = sb[3] * asca;
                         float acc = 0.0f;
                         sp = ns - 1;
                         for (int s = 0; s < ns; ++s) {
@@ -900,7 +916,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         }
                     }
                     float g = T->g[(size_t)sp * nl + p.lam];
-                    float umu = next_u(&p);
+                    float umu = ev[2];
                     float mu;
                     if (fabsf(g) < 1.0e-4f) {
                         mu = 2.0f * umu - 1.0f;
@@ -911,17 +927,18 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         if (mu > 1.0f) mu = 1.0f;
                     }
                     float sn, cs;
-                    orc_sincospif2(next_u(&p), &sn, &cs);
+                    orc_sincospif2(ev[3], &sn, &cs);
                     rotate_dir(&p.kx, &p.ky, &p.kz, mu, cs, sn);
                     cnt->scatterings += 1;
                 } else {
                     /* absorption + reemission */
+                    ev_block(&p, n, RS_SECOND, sb);
                     int sp = 0;
                     if (ns > 1) {
                         float aabs = 0.0f;
                         for (int s = 0; s < ns; ++s)
                             aabs = aabs + X->rho[(size_t)s * G->ncell + c] * T->kabs[(size_t)s * nl + p.lam];
-                        float us = next_u(&p) * aabs;
+                        float us = sb[3] * aabs;
                         float acc = 0.0f;
                         sp = ns - 1;
                         for (int s = 0; s < ns; ++s) {
@@ -930,14 +947,16 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         }
                     }
                     atomic_add64(&DEP(X, p)[(size_t)sp * G->ncell + c], (int64_t)1 << ORC_EUNIT_SHIFT);
-                    p.lam = reemit_lambda(X, &p, sp, c);
-                    iso_dir(&p);
+                    p.lam = reemit_lambda(X, sp, c, sb[0], sb[1], sb[2]);
+                    iso_dir(&p, ev[2], ev[3]);
                     cnt->absorptions += 1;
                 }
-                p.tau = -orc_logf(next_u(&p));
+                p.tau = -orc_logf(ev[1]);
             }
-            if (did_mrw || full)
+            if (did_mrw || (full && !tried))
                 p.dsafe = 0.999999f * (f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p));
+            else if (tried)
+                p.dsafe = 0.999999f * Dw;
             if (p.nevents >= o->max_interactions) { cnt->killed += 1; return p.nevents; }
             if (X->pilot && X->late_after > 0 && p.nevents >= X->late_after) return p.nevents;
         } else {

@@ -32,14 +32,16 @@ class McOptions(C.Structure):
                 ("deadline_ns", C.c_int64), ("abort_flag", C.c_void_p),
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("late_after", C.c_int64), ("time_launches", C.c_int32),
-                ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int32)]
+                ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int32),
+                ("no_batch", C.c_int32), ("drain_below", C.c_int64)]
 
 
 class McStats(C.Structure):
     _fields_ = [("packets", C.c_int64), ("killed", C.c_int64), ("escaped", C.c_int64),
                 ("crossings", C.c_int64), ("events", C.c_int64), ("absorptions", C.c_int64),
                 ("scatterings", C.c_int64), ("mrw_steps", C.c_int64), ("status", C.c_int32),
-                ("launches", C.c_int32), ("parked", C.c_int64), ("late_units", C.c_int64)]
+                ("launches", C.c_int32), ("parked", C.c_int64), ("late_units", C.c_int64),
+                ("drained", C.c_int64)]
 
     def asdict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

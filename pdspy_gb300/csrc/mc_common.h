@@ -29,7 +29,7 @@
 // Stats slots (int64) in the workspace.
 enum {
     ST_PACKETS = 0, ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
-    ST_MRW, ST_STATUS, ST_T0, ST_STOP, ST_LATE, ST_PARKED
+    ST_MRW, ST_STATUS, ST_T0, ST_STOP, ST_LATE, ST_PARKED, ST_DRAINED
 };
 
 // Per-model device descriptor.  Offsets index the plan's double/float pools and the

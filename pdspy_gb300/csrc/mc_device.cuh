@@ -88,21 +88,22 @@ __device__ __forceinline__ void mc_sincospif2(float u, float& sn, float& cs) {
     }
 }
 
-// Per-packet random stream: counter (block, packet, model, pass tag), key = seed.
+// Per-packet random numbers.  Every interaction of a packet owns its own Philox blocks:
+// counter (n, packet, model, pass tag | stream << 24), key = seed, with n the index of the
+// interaction in the packet's life.  Streams: 0 = albedo test, new optical depth, direction
+// cosine, azimuth; 1 = reemission q', reemission row, reemission CDF, species; 2 = MRW
+// diffusion time, jump cosine, jump azimuth; 3 (n = 0) = the emission.  A warp can
+// therefore draw the numbers of future interactions without knowing what happened before
+// them.
+enum { MC_RS_EVENT = 0, MC_RS_SECOND = 1, MC_RS_MRW = 2, MC_RS_EMIT = 3 };
+
 struct McRng {
-    uint32_t pid, model, tag, draw;
-    uint32_t b0, b1, b2, b3;
+    uint32_t pid, model, tag;
 };
 
-__device__ __forceinline__ float mc_next(McRng& r, uint32_t k0, uint32_t k1) {
-    uint32_t i = r.draw & 3u;
-    if (i == 0u) {
-        uint4 o = philox4x32_10(make_uint4(r.draw >> 2, r.pid, r.model, r.tag), k0, k1);
-        r.b0 = o.x; r.b1 = o.y; r.b2 = o.z; r.b3 = o.w;
-    }
-    r.draw += 1u;
-    uint32_t x = (i == 0u) ? r.b0 : (i == 1u) ? r.b1 : (i == 2u) ? r.b2 : r.b3;
-    return mc_u01(x);
+__device__ __forceinline__ uint4 mc_block(const McRng& r, uint32_t n, uint32_t stream, uint32_t k0,
+                                          uint32_t k1) {
+    return philox4x32_10(make_uint4(n, r.pid, r.model, r.tag | (stream << 24)), k0, k1);
 }
 
 // Rotate unit vector k by polar cosine mu and azimuth (cp, sp) about itself.

@@ -50,15 +50,15 @@
 namespace {
 using namespace pdgpu;
 
-// Saved state of a parked packet (everything in the packet except the Philox buffer, which
-// is regenerated from the draw counter).  pos holds the position bits of either geometry.
+// Saved state of a parked packet (its random numbers follow from the packet id and its
+// interaction count).  pos holds the position bits of either geometry.
 struct __align__(16) ParkRec {
     uint64_t pos[3];
     float dsafe, kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events, nevents, ncross;
     int m, epoch;
-    uint32_t pid, model, tag, draw;
+    uint32_t pid, model, tag, spare;
     int pad[3];
 };
 
@@ -85,11 +85,17 @@ struct McParams {
     const float2* q;             // (q_lo, q_span) per [epoch][model][spec][cell]
     int64_t qstride;             // cells per epoch snapshot
     int64_t late_after;          // 0: all deposits go to E
-    ParkRec* park;               // packets parked after late_after events
-    unsigned long long* park_count;
-    int64_t park_cap;
+    ParkRec* park_out;           // phase 0: packets parked after late_after events;
+    unsigned long long* park_out_count;   // phase 1: packets drained for phase 2
+    int64_t park_out_cap;
+    const ParkRec* park_in;      // phases 1 and 2: the packets to resume
+    const unsigned long long* park_in_count;
+    int64_t park_in_cap;
+    unsigned long long* inflight;   // phase 1: packets taken and not yet finished
+    int64_t drain_below;         // phase 1: drain when fewer are in flight (0 = never)
     int32_t pilot;               // pilot pass: packets stop after late_after events
-    int32_t phase;               // 0: epoch launch, 1: continuation of parked packets
+    int32_t phase;               // 0: epoch launch; 1: parked packets, one per thread;
+                                 // 2: drained packets, one per warp (speculative batches)
     int32_t lslot;               // per-launch debug slot
     int64_t* escape;             // [nm][nl] or null
     int64_t* stats;              // [MC_NSTAT]
@@ -106,10 +112,11 @@ struct McParams {
     int32_t dust_floats, use_smem;
     int32_t o_kabs, o_ksca, o_kext, o_g, o_F, o_cdf, o_kP, o_kR, o_mrw;
     int32_t count_stats;
+    int32_t batch;               // continuation: speculative in-cell batches on/off
 };
 
 struct Cnt {
-    long long killed, escaped, crossings, events, absorb, scatter, mrw, late, parked;
+    long long killed, escaped, crossings, events, absorb, scatter, mrw, late, parked, drained;
     int maxev;
 };
 
@@ -252,14 +259,10 @@ struct GeoD {
 // LanePol: one packet per thread (the epoch launches).
 // WarpPol: one packet per warp, its state replicated in all 32 lanes (the continuation of
 // long parked packets, whose sequential chains set the run time).  The lanes share the
-// work that is independent within a step: a window of 32 Philox blocks is generated at
-// once (lane i holds block base+i, a draw is a shuffle), table searches count the entries
-// <= the key with ballots, and the wall candidates are solved on separate lanes.  Every
-// result is identical to the per-thread code; memory side effects are issued by lane 0.
+// work that is independent within a step: table searches count the entries <= the key
+// with ballots, and the wall candidates are solved on separate lanes.  Every result is
+// identical to the per-thread code; memory side effects are issued by lane 0.
 struct LanePol {
-    __device__ __forceinline__ float next(McRng& r, uint32_t k0, uint32_t k1) {
-        return mc_next(r, k0, k1);
-    }
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
         return mc_cdf_search(c, n, u);
     }
@@ -277,23 +280,7 @@ struct LanePol {
 
 struct WarpPol {
     int lane;
-    bool valid;
-    uint32_t base, b0, b1, b2, b3;
-    __device__ __forceinline__ explicit WarpPol(int l) : lane(l), valid(false), base(0) {}
-    __device__ __forceinline__ float next(McRng& r, uint32_t k0, uint32_t k1) {
-        uint32_t blk = r.draw >> 2;
-        if (!valid || blk < base || blk - base >= 32u) {
-            base = blk;
-            uint4 o = philox4x32_10(make_uint4(blk + (uint32_t)lane, r.pid, r.model, r.tag), k0, k1);
-            b0 = o.x; b1 = o.y; b2 = o.z; b3 = o.w;
-            valid = true;
-        }
-        uint32_t i = r.draw & 3u;
-        uint32_t x = (i == 0u) ? b0 : (i == 1u) ? b1 : (i == 2u) ? b2 : b3;
-        x = __shfl_sync(0xffffffffu, x, (int)(blk - base));
-        r.draw += 1u;
-        return mc_u01(x);
-    }
+    __device__ __forceinline__ explicit WarpPol(int l) : lane(l) {}
     // number of entries <= u of a non-decreasing table == smallest index with c > u
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
         int cnt = 0;
@@ -339,30 +326,32 @@ __device__ __forceinline__ float row_interp(Pol& pol, const DustTabs& T, const f
     return tab[j] + w * (tab[j + 1] - tab[j]);
 }
 
+// Reemission wavelength bin of species s from the cell's (q_lo, q_span) snapshot and the
+// three uniforms of the interaction's second stream.
 template <class Pol>
-__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, McRng& rng,
-                                             uint32_t k0, uint32_t k1, float2 q, int s) {
-    float uq = pol.next(rng, k0, k1);
+__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, float2 q, int s,
+                                             float uq, float urow, float ucdf) {
     float qq = q.x + uq * q.y;
     int j;
     float w;
     pol.row(T.F + s * MC_NROW, qq, j, w);
-    int row = j + ((pol.next(rng, k0, k1) < w) ? 1 : 0);
-    return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, pol.next(rng, k0, k1));
+    int row = j + ((urow < w) ? 1 : 0);
+    return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, ucdf);
 }
 
 template <class G>
 __device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, const float* star_cdf,
                                      int nl, uint32_t k0, uint32_t k1) {
-    float mu = 2.0f * mc_next(p.rng, k0, k1) - 1.0f;
+    const uint4 e = mc_block(p.rng, 0u, MC_RS_EMIT, k0, k1);
+    float mu = 2.0f * mc_u01(e.x) - 1.0f;
     float sn, cs;
-    mc_sincospif2(mc_next(p.rng, k0, k1), sn, cs);
+    mc_sincospif2(mc_u01(e.y), sn, cs);
     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
     p.kx = st * cs;
     p.ky = st * sn;
     p.kz = mu;
-    p.lam = mc_cdf_search(star_cdf, nl, mc_next(p.rng, k0, k1));
-    p.tau = -mc_logf(mc_next(p.rng, k0, k1));
+    p.lam = mc_cdf_search(star_cdf, nl, mc_u01(e.z));
+    p.tau = -mc_logf(mc_u01(e.w));
     G::origin(p);
     p.dsafe = 0.0f;
     p.ir = -1; p.itv = 0; p.ip = 0;
@@ -370,6 +359,29 @@ __device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, cons
     p.cell_events = 0;
     p.nevents = 0;
     p.ncross = 0;
+}
+
+template <class G>
+__device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p) {
+    G::save(r, p);
+    r.dsafe = p.dsafe;
+    r.kx = p.kx; r.ky = p.ky; r.kz = p.kz; r.tau = p.tau;
+    r.ir = p.ir; r.itv = p.itv; r.ip = p.ip; r.lam = p.lam;
+    r.last_wall = p.last_wall; r.cell_events = p.cell_events;
+    r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
+    r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag; r.spare = 0;
+    r.pad[0] = 0; r.pad[1] = 0; r.pad[2] = 0;
+}
+
+template <class G>
+__device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r) {
+    G::load(p, r);
+    p.dsafe = r.dsafe;
+    p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
+    p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
+    p.last_wall = r.last_wall; p.cell_events = r.cell_events;
+    p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
+    p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag;
 }
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
@@ -419,18 +431,24 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         G::move(p, se, p.kx, p.ky, p.kz);
         p.dsafe = full ? 0.0f : p.dsafe - sef;
         p.last_wall = W_NONE;
+        const uint32_t n = (uint32_t)p.nevents;   // index of this interaction
         p.cell_events += 1;
         p.nevents += 1;
         cnt.events += 1;
         const bool late = P.late_after > 0 && p.nevents > P.late_after;
         int64_t* dep = late ? P.Elate : P.E;
         const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
+        const uint4 ev = mc_block(p.rng, n, MC_RS_EVENT, k0, k1);
         bool did_mrw = false;
         // MRW is tried after mrw_count_trigger events in one cell, and at every event once
-        // the packet has made more than mrw_eager_after events (it is trapped).
-        if (P.mrw && (p.cell_events >= P.mrw_trigger ||
-                      (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after))) {
-            float R0f = 0.999f * G::dist(M, dp, P.fpool, p);
+        // the packet has made more than mrw_eager_after events (it is trapped).  The wall
+        // distance of a try also refreshes the safety distance.
+        const bool tried = P.mrw && (p.cell_events >= P.mrw_trigger ||
+                                     (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after));
+        float Dw = 0.0f;
+        if (tried) {
+            Dw = G::dist(M, dp, P.fpool, p);
+            float R0f = 0.999f * Dw;
             len_t R0 = G::of(R0f);
             float2 qv[NS];
             float aR = 0.0f;
@@ -441,7 +459,9 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
             }
             if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
                 did_mrw = true;
-                float uy = pol.next(p.rng, k0, k1);
+                const uint4 mb = mc_block(p.rng, n, MC_RS_MRW, k0, k1);
+                const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
+                float uy = mc_u01(mb.x);
                 float f = uy * (float)(MC_NMRW - 1);
                 int i = (int)f;
                 if (i > MC_NMRW - 2) i = MC_NMRW - 2;
@@ -463,24 +483,24 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 float dx, dy, dz;
                 {
-                    float mu = 2.0f * pol.next(p.rng, k0, k1) - 1.0f;
+                    float mu = 2.0f * mc_u01(mb.y) - 1.0f;
                     float sn, cs;
-                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(mc_u01(mb.z), sn, cs);
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     dx = st * cs; dy = st * sn; dz = mu;
                 }
                 G::move(p, R0, dx, dy, dz);
                 {
-                    float mu = sqrtf(pol.next(p.rng, k0, k1));
+                    float mu = sqrtf(mc_u01(ev.z));
                     float sn, cs;
-                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(mc_u01(ev.w), sn, cs);
                     float kx = dx, ky = dy, kz = dz;
                     mc_rotate(kx, ky, kz, mu, cs, sn);
                     p.kx = kx; p.ky = ky; p.kz = kz;
                 }
                 int sp = 0;
                 if (NS > 1) {
-                    float us = pol.next(p.rng, k0, k1) * aP;
+                    float us = mc_u01(sb.w) * aP;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -493,21 +513,22 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
 #pragma unroll
                 for (int s = 1; s < NS; ++s)
                     if (s == sp) qs = qv[s];
-                p.lam = reemit_lambda(pol, T, nl, p.rng, k0, k1, qs, sp);
-                p.tau = -mc_logf(pol.next(p.rng, k0, k1));
+                p.lam = reemit_lambda(pol, T, nl, qs, sp, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
+                p.tau = -mc_logf(mc_u01(ev.y));
                 p.cell_events = 0;
                 cnt.mrw += 1;
             }
         }
         if (!did_mrw) {
-            float ua = pol.next(p.rng, k0, k1);
+            float ua = mc_u01(ev.x);
             float asca = 0.0f;
 #pragma unroll
             for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + p.lam];
             if (ua * alpha < asca) {
                 int sp = 0;
                 if (NS > 1) {
-                    float us = pol.next(p.rng, k0, k1) * asca;
+                    const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
+                    float us = mc_u01(sb.w) * asca;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -517,7 +538,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                     }
                 }
                 float g = T.g[sp * nl + p.lam];
-                float umu = pol.next(p.rng, k0, k1);
+                float umu = mc_u01(ev.z);
                 float mu;
                 if (fabsf(g) < 1.0e-4f) {
                     mu = 2.0f * umu - 1.0f;
@@ -528,16 +549,17 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                     if (mu > 1.0f) mu = 1.0f;
                 }
                 float sn, cs;
-                mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
+                mc_sincospif2(mc_u01(ev.w), sn, cs);
                 mc_rotate(p.kx, p.ky, p.kz, mu, cs, sn);
                 cnt.scatter += 1;
             } else {
+                const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
                 int sp = 0;
                 if (NS > 1) {
                     float aabs = 0.0f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + p.lam];
-                    float us = pol.next(p.rng, k0, k1) * aabs;
+                    float us = mc_u01(sb.w) * aabs;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -548,19 +570,21 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
-                p.lam = reemit_lambda(pol, T, nl, p.rng, k0, k1, qa[idx], sp);
+                p.lam = reemit_lambda(pol, T, nl, qa[idx], sp, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
                 {
-                    float mu = 2.0f * pol.next(p.rng, k0, k1) - 1.0f;
+                    float mu = 2.0f * mc_u01(ev.z) - 1.0f;
                     float sn, cs;
-                    mc_sincospif2(pol.next(p.rng, k0, k1), sn, cs);
+                    mc_sincospif2(mc_u01(ev.w), sn, cs);
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
                     p.kx = st * cs; p.ky = st * sn; p.kz = mu;
                 }
                 cnt.absorb += 1;
             }
-            p.tau = -mc_logf(pol.next(p.rng, k0, k1));
+            p.tau = -mc_logf(mc_u01(ev.y));
         }
-        if (did_mrw || full) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
+        if (did_mrw) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
+        else if (tried) p.dsafe = 0.999999f * Dw;
+        else if (full) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
         if (late) cnt.late += 1;
         if (p.nevents >= P.max_inter) {
             cnt.killed += 1;
@@ -568,18 +592,11 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         }
         if (P.late_after > 0 && p.nevents == P.late_after && P.phase == 0) {
             if (P.pilot) return false;   // later deposits of pilot packets are discarded
-            unsigned long long slot = atomicAdd(P.park_count, 1ull);
-            if ((long long)slot < P.park_cap) {
+            unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
+            if ((long long)slot < P.park_out_cap) {
                 ParkRec r;
-                G::save(r, p);
-                r.dsafe = p.dsafe;
-                r.kx = p.kx; r.ky = p.ky; r.kz = p.kz; r.tau = p.tau;
-                r.ir = p.ir; r.itv = p.itv; r.ip = p.ip; r.lam = p.lam;
-                r.last_wall = p.last_wall; r.cell_events = p.cell_events;
-                r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
-                r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag; r.draw = p.rng.draw;
-                r.pad[0] = 0; r.pad[1] = 0;
-                P.park[slot] = r;
+                park_save<G>(r, p);
+                P.park_out[slot] = r;
                 cnt.parked += 1;
                 return false;
             }
@@ -617,6 +634,297 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     return true;
 }
 
+// Shuffle of a register-resident struct, word by word.
+template <class S>
+__device__ __forceinline__ S shfl_struct(const S& v, int src) {
+    static_assert(sizeof(S) % 4 == 0, "word-sized struct");
+    S out;
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(&v);
+    uint32_t* b = reinterpret_cast<uint32_t*>(&out);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(S) / 4); ++i) b[i] = __shfl_sync(0xffffffffu, a[i], src);
+    return out;
+}
+
+// Speculative batch of in-cell interactions of one packet owned by a whole warp.
+//
+// Because every interaction draws from its own Philox blocks, lane j can prepare
+// interaction n0 + j before the ones in front of it are known: its random numbers, the new
+// optical depth, the isotropic direction and the reemission wavelength an absorption would
+// give (the cell, and so its temperature snapshot, is fixed inside a batch).  One cheap
+// sequential pass then chains wavelength, direction and position through the batch
+// assuming every interaction stays in the cell; the expensive checks run on all lanes at
+// once: the wall distance after each interaction (MRW test and safety-distance refresh)
+// and, for interactions that the safety distance cannot clear, the full wall solve.  The
+// first MRW jump ends the batch and is carried out by its lane with the values already at
+// hand.  The batch is cut before the first interaction that leaves the cell or is placed
+// on a wall; the caller runs that one through the general step.  The committed
+// interactions are identical, operation for operation, to running the general step one by
+// one.
+//
+// Returns the number of interactions committed and sets *cut when the batch stopped
+// before an interaction that needs the general step; returns -1 when the packet's state
+// does not allow a batch.
+template <int NS, class G>
+__device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt,
+                         int lane, bool* cut) {
+    using Pk = typename G::Pkt;
+    using len_t = typename G::len_t;
+    const unsigned FULL = 0xffffffffu;
+    *cut = true;
+    if (p.ir < 0) return -1;
+    const McModel& M = P.models[p.m];
+    const double* __restrict__ dp = P.dpool;
+    const int nl = P.nl;
+    const uint32_t k0 = P.key0, k1 = P.key1;
+    int B = 32;
+    const long long room = (long long)P.max_inter - 1 - (long long)p.nevents;
+    if (room < (long long)B) B = room > 0 ? (int)room : 0;
+    if (B <= 0) return -1;
+    const int c = G::cell(M, p);
+    const int64_t base = M.cell_off;
+    float rh[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) rh[s] = __ldg(P.rho + base + (int64_t)s * M.ncell + c);
+    const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
+    float2 qv[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) qv[s] = qa[base + (int64_t)s * M.ncell + c];
+    LanePol lp;
+    float aR = 0.0f;
+    if (P.mrw) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            aR = aR + rh[s] * row_interp(lp, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+    }
+    // phase 1: lane j prepares interaction n0 + j
+    const uint32_t n0 = (uint32_t)p.nevents;
+    float ua = 0.0f, tn = 0.0f, umu = 0.0f, cs = 1.0f, sn = 0.0f, kix = 0.0f, kiy = 0.0f,
+          kiz = 1.0f, us = 0.0f;
+    int la[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) la[s] = 0;
+    if (lane < B) {
+        const uint4 ev = mc_block(p.rng, n0 + (uint32_t)lane, MC_RS_EVENT, k0, k1);
+        const uint4 sb = mc_block(p.rng, n0 + (uint32_t)lane, MC_RS_SECOND, k0, k1);
+        ua = mc_u01(ev.x);
+        tn = -mc_logf(mc_u01(ev.y));
+        umu = mc_u01(ev.z);
+        mc_sincospif2(mc_u01(ev.w), sn, cs);
+        float mu = 2.0f * umu - 1.0f;
+        float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+        kix = st * cs; kiy = st * sn; kiz = mu;
+        us = mc_u01(sb.w);
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            la[s] = reemit_lambda(lp, T, nl, qv[s], s, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
+    }
+    // phase 2: sequential chain, identical in every lane; lane j keeps interaction j
+    Pk q = p;
+    Pk pre = p, post = p;
+    float my_alpha = 0.0f, my_sef = 0.0f;
+    int my_abs = 0, my_sp = 0;
+    for (int j = 0; j < B; ++j) {
+        float a = 0.0f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) a = a + rh[s] * T.kext[s * nl + q.lam];
+        if (!(a > 0.0f)) { B = j; break; }
+        const float sef = q.tau / a;
+        if (lane == j) { pre = q; my_alpha = a; my_sef = sef; }
+        G::move(q, G::of(sef), q.kx, q.ky, q.kz);
+        q.last_wall = W_NONE;
+        q.cell_events += 1;
+        q.nevents += 1;
+        const float ua_j = __shfl_sync(FULL, ua, j);
+        const float us_j = (NS > 1) ? __shfl_sync(FULL, us, j) : 0.0f;
+        float asca = 0.0f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + q.lam];
+        if (ua_j * a < asca) {
+            int sp = 0;
+            if (NS > 1) {
+                float usv = us_j * asca;
+                float acc = 0.0f;
+                sp = NS - 1;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    acc = acc + rh[s] * T.ksca[s * nl + q.lam];
+                    if (usv < acc) { sp = s; break; }
+                }
+            }
+            const float g = T.g[sp * nl + q.lam];
+            const float umu_j = __shfl_sync(FULL, umu, j);
+            const float cs_j = __shfl_sync(FULL, cs, j);
+            const float sn_j = __shfl_sync(FULL, sn, j);
+            float mu;
+            if (fabsf(g) < 1.0e-4f) {
+                mu = 2.0f * umu_j - 1.0f;
+            } else {
+                float t = (1.0f - g * g) / (1.0f - g + 2.0f * g * umu_j);
+                mu = (1.0f + g * g - t * t) / (2.0f * g);
+                if (mu < -1.0f) mu = -1.0f;
+                if (mu > 1.0f) mu = 1.0f;
+            }
+            mc_rotate(q.kx, q.ky, q.kz, mu, cs_j, sn_j);
+            if (lane == j) my_abs = 0;
+        } else {
+            int sp = 0;
+            if (NS > 1) {
+                float aabs = 0.0f;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + q.lam];
+                float usv = us_j * aabs;
+                float acc = 0.0f;
+                sp = NS - 1;
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    acc = acc + rh[s] * T.kabs[s * nl + q.lam];
+                    if (usv < acc) { sp = s; break; }
+                }
+            }
+            int lsel = la[0];
+#pragma unroll
+            for (int s = 1; s < NS; ++s)
+                if (s == sp) lsel = la[s];
+            q.lam = __shfl_sync(FULL, lsel, j);
+            q.kx = __shfl_sync(FULL, kix, j);
+            q.ky = __shfl_sync(FULL, kiy, j);
+            q.kz = __shfl_sync(FULL, kiz, j);
+            if (lane == j) { my_abs = 1; my_sp = sp; }
+        }
+        q.tau = __shfl_sync(FULL, tn, j);
+        if (lane == j) post = q;
+    }
+    if (B <= 0) return -1;
+    // phase 3: wall distance after each interaction and the MRW test
+    float D = 0.0f;
+    bool tried = false, ok = false;
+    if (lane < B) {
+        tried = P.mrw && (post.cell_events >= P.mrw_trigger ||
+                          (P.mrw_eager_after > 0 && post.nevents > P.mrw_eager_after));
+        D = G::dist(M, dp, P.fpool, post);
+        const float R0f = 0.999f * D;
+        ok = tried && (R0f * aR >= P.mrw_gamma && R0f * my_alpha >= P.mrw_tauthres);
+    }
+    const unsigned live = (B >= 32) ? FULL : ((1u << B) - 1u);
+    const unsigned okm = __ballot_sync(FULL, ok) & live;
+    const int Jm = okm ? (__ffs(okm) - 1) : B;   // first MRW jump
+    // phase 4: safety-distance replay (which interactions need a wall solve)
+    float dsf = p.dsafe;
+    bool my_full = false;
+    float my_dsafe = 0.0f;
+    const int Jr = Jm < B ? Jm + 1 : B;
+    for (int j = 0; j < Jr; ++j) {
+        const float sef_j = __shfl_sync(FULL, my_sef, j);
+        const float D_j = __shfl_sync(FULL, D, j);
+        const bool tr_j = __shfl_sync(FULL, tried, j);
+        const bool full = !(sef_j < dsf);
+        dsf = (full || tr_j) ? 0.999999f * D_j : dsf - sef_j;
+        if (lane == j) { my_full = full; my_dsafe = dsf; }
+    }
+    // phase 5: wall solves of the interactions the safety distance did not clear
+    bool bad = false;
+    if (lane < Jr && my_full) {
+        int w;
+        const len_t sw = G::wall_lane(M, dp, P.fpool, pre, w);
+        const float tcell = my_alpha * G::f(sw);
+        bad = !(tcell > pre.tau) || G::gt(G::of(my_sef), sw);
+    }
+    const unsigned badm = __ballot_sync(FULL, bad) & live;
+    const int Jb = badm ? (__ffs(badm) - 1) : B;
+    const bool jump = Jm < B && Jb > Jm;    // the batch ends with an MRW jump
+    const int J = jump ? Jm : min(Jm, Jb);
+    *cut = !jump && J < B;
+    // commit interactions 0..J-1
+    const bool mine = lane < J;
+    const bool late = P.late_after > 0 && post.nevents > P.late_after;
+    if (mine && my_abs) {
+        int64_t* dep = late ? P.Elate : P.E;
+        atomicAdd((unsigned long long*)(dep + base + (int64_t)my_sp * M.ncell + c),
+                  1ull << MC_EUNIT_SHIFT);
+    }
+    const int nabs = __popc(__ballot_sync(FULL, mine && my_abs));
+    const int nlate = __popc(__ballot_sync(FULL, mine && late));
+    cnt.events += J;
+    cnt.absorb += nabs;
+    cnt.scatter += J - nabs;
+    cnt.late += nlate;
+    if (!jump) {
+        if (J > 0) {
+            p = shfl_struct(post, J - 1);
+            p.dsafe = __shfl_sync(FULL, my_dsafe, J - 1);
+        }
+        return J;
+    }
+    // the MRW jump of interaction Jm, computed by its lane (as in the general step)
+    Pk m = post;
+    if (lane == Jm) {
+        const uint4 mb = mc_block(p.rng, n0 + (uint32_t)Jm, MC_RS_MRW, k0, k1);
+        const float R0f = 0.999f * D;
+        const len_t R0 = G::of(R0f);
+        float uy = mc_u01(mb.x);
+        float f = uy * (float)(MC_NMRW - 1);
+        int i = (int)f;
+        if (i > MC_NMRW - 2) i = MC_NMRW - 2;
+        float w = f - (float)i;
+        float yv = T.mrw[i] + w * (T.mrw[i + 1] - T.mrw[i]);
+        float ell = 3.0f * aR * R0f * R0f * yv;
+        int64_t* dep = late ? P.Elate : P.E;
+        float kp[NS];
+        float aP = 0.0f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            kp[s] = rh[s] * row_interp(lp, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+            aP = aP + kp[s];
+            float units_f = kp[s] * ell * 1048576.0f + 0.5f;
+            if (units_f > 9.0e18f) units_f = 9.0e18f;
+            long long units = (long long)units_f;
+            if (units > 0)
+                atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
+                          (unsigned long long)units);
+        }
+        float dx, dy, dz;
+        {
+            float mu = 2.0f * mc_u01(mb.y) - 1.0f;
+            float sn2, cs2;
+            mc_sincospif2(mc_u01(mb.z), sn2, cs2);
+            float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+            dx = st * cs2; dy = st * sn2; dz = mu;
+        }
+        G::move(m, R0, dx, dy, dz);
+        {
+            float mu = sqrtf(umu);
+            float kx = dx, ky = dy, kz = dz;
+            mc_rotate(kx, ky, kz, mu, cs, sn);
+            m.kx = kx; m.ky = ky; m.kz = kz;
+        }
+        int sp = 0;
+        if (NS > 1) {
+            float usv = us * aP;
+            float acc = 0.0f;
+            sp = NS - 1;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                acc = acc + kp[s];
+                if (usv < acc) { sp = s; break; }
+            }
+        }
+        int lsel = la[0];
+#pragma unroll
+        for (int s = 1; s < NS; ++s)
+            if (s == sp) lsel = la[s];
+        m.lam = lsel;
+        m.tau = tn;
+        m.cell_events = 0;
+        m.dsafe = 0.999999f * G::dist(M, dp, P.fpool, m);
+    }
+    p = shfl_struct(m, Jm);
+    cnt.events += 1;
+    cnt.mrw += 1;
+    if (__shfl_sync(FULL, late, Jm)) cnt.late += 1;
+    return J + 1;
+}
+
 __device__ __forceinline__ long long warp_sum(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -640,8 +948,8 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
         s_stop = (*(volatile long long*)(P.stats + ST_STOP) != 0) ? 1 : 0;
         long long tot = P.total;
         if (P.phase == 1) {
-            long long c = (long long)*(volatile unsigned long long*)P.park_count;
-            tot = c < P.park_cap ? c : P.park_cap;
+            long long c = (long long)*(volatile const unsigned long long*)P.park_in_count;
+            tot = c < P.park_in_cap ? c : P.park_in_cap;
         }
         s_total = tot;
         atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
@@ -663,43 +971,83 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
 
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     typename G::Pkt p;
     bool active = false;
     unsigned iter = 0;
     LanePol lanepol;
+    bool queue_open = true;
     for (;;) {
         if (s_stop) break;
-        unsigned need = __ballot_sync(0xffffffffu, !active);
+        unsigned need = queue_open ? __ballot_sync(0xffffffffu, !active) : 0u;
         if (need) {
             int n = __popc(need);
             unsigned long long basev = 0;
             if (lane == 0) basev = atomicAdd(P.queue, (unsigned long long)n);
             basev = __shfl_sync(0xffffffffu, basev, 0);
+            if ((long long)basev + n >= total) queue_open = false;
+            bool got = false;
             if (!active) {
                 long long g = (long long)basev + __popc(need & lt_mask);
                 if (g < total) {
-                    int lo = 0, hi = P.nm;
-                    while (hi - lo > 1) {
-                        int mid = (lo + hi) >> 1;
-                        if (s_cum[mid] <= g) lo = mid; else hi = mid;
+                    if (P.phase == 1) {
+                        park_load<G>(p, P.park_in[g]);
+                    } else {
+                        int lo = 0, hi = P.nm;
+                        while (hi - lo > 1) {
+                            int mid = (lo + hi) >> 1;
+                            if (s_cum[mid] <= g) lo = mid; else hi = mid;
+                        }
+                        const McModel& M = P.models[lo];
+                        p.m = lo;
+                        p.epoch = P.epoch;
+                        p.rng.pid = (uint32_t)(M.bnd[P.epoch] + (g - s_cum[lo]));
+                        p.rng.model = (uint32_t)M.model_id;
+                        p.rng.tag = P.tag;
+                        emit<G>(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
                     }
-                    const McModel& M = P.models[lo];
-                    p.m = lo;
-                    p.epoch = P.epoch;
-                    p.rng.pid = (uint32_t)(M.bnd[P.epoch] + (g - s_cum[lo]));
-                    p.rng.model = (uint32_t)M.model_id;
-                    p.rng.tag = P.tag;
-                    p.rng.draw = 0;
-                    emit<G>(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
                     active = true;
+                    got = true;
                 }
+            }
+            if (P.phase == 1) {
+                int ng = __popc(__ballot_sync(0xffffffffu, got));
+                if (lane == 0 && ng) atomicAdd(P.inflight, (unsigned long long)ng);
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
+        const bool was = active;
         if (active) {
             active = mc_step<NS, LanePol, G>(p, P, T, cnt, lanepol);
             if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
+        }
+        if (P.phase == 1) {
+            int nf = __popc(__ballot_sync(0xffffffffu, was && !active));
+            if (lane == 0 && nf) atomicAdd(P.inflight, (unsigned long long)(-(long long)nf));
+            // few packets left: hand them to the warp-per-packet launch
+            if (!queue_open && P.drain_below > 0 && (iter & 63u) == 63u) {
+                int dr = 0;
+                if (lane == 0)
+                    dr = (long long)*(volatile unsigned long long*)P.inflight < P.drain_below;
+                dr = __shfl_sync(0xffffffffu, dr, 0);
+                if (dr) {
+                    bool parked = false;
+                    if (active) {
+                        unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
+                        if ((long long)slot < P.park_out_cap) {
+                            ParkRec r;
+                            park_save<G>(r, p);
+                            P.park_out[slot] = r;
+                            parked = true;
+                            active = false;
+                            cnt.drained += 1;
+                        }
+                    }
+                    int np = __popc(__ballot_sync(0xffffffffu, parked));
+                    if (lane == 0 && np) atomicAdd(P.inflight, (unsigned long long)(-(long long)np));
+                    if (!__any_sync(0xffffffffu, active)) break;
+                }
+            }
         }
         if (((++iter) & 4095u) == 0u) {
             int stop = 0;
@@ -723,12 +1071,12 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
         }
     }
     if (P.count_stats) {
-        long long v[9] = {cnt.killed, cnt.escaped, cnt.crossings, cnt.events, cnt.absorb,
-                          cnt.scatter, cnt.mrw, cnt.late, cnt.parked};
-        const int slot[9] = {ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
-                             ST_MRW, ST_LATE, ST_PARKED};
+        long long v[10] = {cnt.killed, cnt.escaped, cnt.crossings, cnt.events, cnt.absorb,
+                           cnt.scatter, cnt.mrw, cnt.late, cnt.parked, cnt.drained};
+        const int slot[10] = {ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
+                              ST_MRW, ST_LATE, ST_PARKED, ST_DRAINED};
 #pragma unroll
-        for (int i = 0; i < 9; ++i) {
+        for (int i = 0; i < 10; ++i) {
             long long s = warp_sum(v[i]);
             if (lane == 0 && s) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)s);
         }
@@ -754,8 +1102,8 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
     __shared__ long long s_total;
     if (threadIdx.x == 0) {
         s_stop = (*(volatile long long*)(P.stats + ST_STOP) != 0) ? 1 : 0;
-        long long c = (long long)*(volatile unsigned long long*)P.park_count;
-        s_total = c < P.park_cap ? c : P.park_cap;
+        long long c = (long long)*(volatile const unsigned long long*)P.park_in_count;
+        s_total = c < P.park_in_cap ? c : P.park_in_cap;
         atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
     }
     const float* tab = P.fpool;
@@ -772,7 +1120,7 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
     T.F = tab + P.o_F; T.cdf = tab + P.o_cdf; T.kP = tab + P.o_kP; T.kR = tab + P.o_kR;
     T.mrw = tab + P.o_mrw;
     const int lane = threadIdx.x & 31;
-    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Cnt cnt = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool stop = s_stop != 0;
     unsigned iter = 0;
     while (!stop) {
@@ -780,19 +1128,14 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         if (lane == 0) g = atomicAdd(P.queue, 1ull);
         g = __shfl_sync(0xffffffffu, g, 0);
         if ((long long)g >= total) break;
-        const ParkRec r = P.park[g];
         typename G::Pkt p;
-        G::load(p, r);
-        p.dsafe = r.dsafe;
-        p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
-        p.ir = r.ir; p.itv = r.itv; p.ip = r.ip; p.lam = r.lam;
-        p.last_wall = r.last_wall; p.cell_events = r.cell_events;
-        p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
-        p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag; p.rng.draw = r.draw;
+        park_load<G>(p, P.park_in[g]);
         WarpPol pol(lane);
         bool alive = true;
         while (alive) {
-            alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
+            bool cut = true;
+            if (P.batch) seb_batch<NS, G>(p, P, T, cnt, lane, &cut);
+            if (cut) alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
                 if (lane == 0) {
@@ -953,7 +1296,7 @@ struct pdgpu_mc_plan {
     int64_t total_cells, total_nphot;
     // workspace layout
     size_t ws_fpool, ws_dpool, ws_models, ws_cum, ws_E, ws_D, ws_q, ws_escape, ws_stats,
-        ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_parkcnt;
+        ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_park2, ws_parkcnt;
     int64_t park_cap;
     int nqueue;
     int device, nsm, block, grid;
@@ -1136,7 +1479,7 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->K = options->nepoch < 1 ? 1 : std::min(options->nepoch, MC_MAX_EPOCH);
     P->npilot = std::max(0, options->npilot);
     P->K = std::min(P->K, MC_MAX_LAUNCH - 2);
-    P->npilot = std::min(P->npilot, MC_MAX_LAUNCH - 1 - P->K);
+    P->npilot = std::min(P->npilot, MC_MAX_LAUNCH - 2 - P->K);   // K + npilot + 2 launches
     // fewer epochs when a model has too few packets for the first epoch to be non-empty
     for (int m = 0; m < nmodels; ++m)
         while (P->K > 1 && (models[m].nphot >> (P->K - 1)) == 0) P->K--;
@@ -1246,10 +1589,12 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->ws_Elate = place((size_t)P->total_cells * sizeof(int64_t));
     P->park_cap = std::max<int64_t>(8192, P->total_nphot / 128);
     P->ws_park = place((size_t)P->park_cap * sizeof(ParkRec));
-    P->ws_parkcnt = place(sizeof(unsigned long long));
+    P->ws_park2 = place((size_t)P->park_cap * sizeof(ParkRec));
+    // [parked after late_after, drained for the warp-per-packet launch, in flight, spare]
+    P->ws_parkcnt = place(4 * sizeof(unsigned long long));
     P->ws_escape = place((size_t)nmodels * nl * sizeof(int64_t));
     P->ws_stats = place(MC_NSTAT * sizeof(int64_t));
-    P->nqueue = P->K + P->npilot + 1;
+    P->nqueue = P->K + P->npilot + 2;   // one work counter per launch
     P->ws_queue = place((size_t)P->nqueue * sizeof(unsigned long long));
     P->ws_total = (o + 255) / 256 * 256;
     P->uploaded_ws = nullptr;
@@ -1337,9 +1682,17 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.q = (const float2*)(w + P->ws_q);
     prm.qstride = P->total_cells;
     prm.late_after = P->opt.late_after > 0 ? P->opt.late_after : 0;
-    prm.park = (ParkRec*)(w + P->ws_park);
-    prm.park_count = (unsigned long long*)(w + P->ws_parkcnt);
-    prm.park_cap = P->park_cap;
+    unsigned long long* counts = (unsigned long long*)(w + P->ws_parkcnt);
+    ParkRec* listA = (ParkRec*)(w + P->ws_park);
+    ParkRec* listB = (ParkRec*)(w + P->ws_park2);
+    prm.park_out = phase == 0 ? listA : listB;
+    prm.park_out_count = phase == 0 ? counts : counts + 1;
+    prm.park_out_cap = P->park_cap;
+    prm.park_in = phase == 1 ? listA : listB;
+    prm.park_in_count = phase == 1 ? counts : counts + 1;
+    prm.park_in_cap = P->park_cap;
+    prm.inflight = counts + 2;
+    prm.drain_below = 0;
     prm.pilot = final_pass ? 0 : 1;
     prm.phase = phase;
     prm.lslot = lslot;
@@ -1349,6 +1702,25 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.abort_flag = P->opt.abort_flag;
     prm.deadline_ns = P->opt.deadline_ns;
     prm.total = phase == 0 ? P->cum[(size_t)epoch * (P->nm + 1) + P->nm] : P->park_cap;
+    if (phase == 1 && P->opt.drain_below >= 0) {
+        int64_t d = P->opt.drain_below;
+        if (d == 0) {
+            // as many packets as the warp-per-packet launch keeps running at once
+            void (*ck)(McParams) = nullptr;
+            switch (P->ns) {
+                case 1: ck = P->opt.fp64_walls ? mc_continue_kernel<1, GeoD> : mc_continue_kernel<1, GeoS>; break;
+                case 2: ck = P->opt.fp64_walls ? mc_continue_kernel<2, GeoD> : mc_continue_kernel<2, GeoS>; break;
+                case 3: ck = P->opt.fp64_walls ? mc_continue_kernel<3, GeoD> : mc_continue_kernel<3, GeoS>; break;
+                default: ck = P->opt.fp64_walls ? mc_continue_kernel<4, GeoD> : mc_continue_kernel<4, GeoS>; break;
+            }
+            int per = 0;
+            if (cudaFuncSetAttribute(ck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem_bytes) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ck, P->block, P->smem_bytes) != cudaSuccess)
+                return PDGPU_CUDA_ERROR;
+            d = (int64_t)std::max(per, 1) * P->nsm * (P->block / 32);
+        }
+        prm.drain_below = d;
+    }
     prm.nm = P->nm;
     prm.ns = P->ns;
     prm.nl = P->nl;
@@ -1370,10 +1742,11 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.o_F = P->o_F; prm.o_cdf = P->o_cdf; prm.o_kP = P->o_kP; prm.o_kR = P->o_kR;
     prm.o_mrw = P->o_mrw;
     prm.count_stats = final_pass ? 1 : 0;
+    prm.batch = P->opt.no_batch ? 0 : 1;
     if (prm.total <= 0) return PDGPU_OK;
     void (*kern)(McParams) = nullptr;
     const bool f64 = P->opt.fp64_walls != 0;
-    if (phase == 0) {
+    if (phase <= 1) {
         switch (P->ns) {
             case 1: kern = f64 ? mc_transport_kernel<1, GeoD> : mc_transport_kernel<1, GeoS>; break;
             case 2: kern = f64 ? mc_transport_kernel<2, GeoD> : mc_transport_kernel<2, GeoS>; break;
@@ -1401,7 +1774,7 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     if (P->opt.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)P->opt.blocks_per_sm);
     int64_t want = (prm.total + P->block - 1) / P->block;
     int grid = (int)std::min<int64_t>((int64_t)per_sm * P->nsm, std::max<int64_t>(want, 1));
-    if (phase == 1) grid = per_sm * P->nsm;  // parked count is only known on the device
+    if (phase >= 1) grid = per_sm * P->nsm;  // parked count is only known on the device
     P->grid = grid;
     if (P->opt.time_launches && P->ev_ready) cudaEventRecord(P->ev[2 * lslot], st);
     kern<<<grid, P->block, P->smem_bytes, st>>>(prm);
@@ -1444,7 +1817,7 @@ pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* P, const float* rho, double* tempe
     if (cudaMemsetAsync(E, 0, cells_bytes, st) != cudaSuccess ||
         cudaMemsetAsync(D, 0, cells_bytes, st) != cudaSuccess ||
         cudaMemsetAsync(EL, 0, cells_bytes, st) != cudaSuccess ||
-        cudaMemsetAsync(w + P->ws_parkcnt, 0, sizeof(unsigned long long), st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_parkcnt, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_escape, 0, (size_t)P->nm * P->nl * sizeof(int64_t), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_stats, 0, MC_NSTAT * sizeof(int64_t), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_queue, 0, (size_t)P->nqueue * sizeof(unsigned long long), st) !=
@@ -1469,9 +1842,12 @@ pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* P, const float* rho, double* tempe
         if ((rc = launch_prep(P, w, rho, E, 0, k, st)) != PDGPU_OK) return rc;
         if ((rc = launch_transport(P, w, rho, E, k, 0u, lslot++, true, 0, st)) != PDGPU_OK) return rc;
     }
-    // packets parked after late_after events finish here, each with its epoch's snapshot
-    if (P->opt.late_after > 0)
+    // packets parked after late_after events finish here, each with its epoch's snapshot:
+    // one per thread while there are many, the last few one per warp
+    if (P->opt.late_after > 0) {
         if ((rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 1, st)) != PDGPU_OK) return rc;
+        if ((rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 2, st)) != PDGPU_OK) return rc;
+    }
     TempParams tp;
     tp.models = (const McModel*)(w + P->ws_models);
     tp.dpool = (const double*)(w + P->ws_dpool);
@@ -1507,8 +1883,9 @@ pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* P, const void* ws, void* stream,
     S->scatterings = h[ST_SCATTER];
     S->mrw_steps = h[ST_MRW];
     S->status = (int32_t)h[ST_STATUS];
-    S->launches = P->K + P->npilot + (P->opt.late_after > 0 ? 1 : 0);
+    S->launches = P->K + P->npilot + (P->opt.late_after > 0 ? 2 : 0);
     S->parked = h[ST_PARKED];
+    S->drained = h[ST_DRAINED];
     S->late_units = h[ST_LATE];
     return PDGPU_OK;
 }

@@ -140,7 +140,7 @@ class ThermalPlan:
                  max_interactions=DEFAULTS["max_interactions"], late_after=DEFAULTS["late_after"],
                  mrw_eager_after=DEFAULTS["mrw_eager_after"], timelimit=None, device=None,
                  block_threads=0, blocks_per_sm=0, abort_flag=None, time_launches=False,
-                 fp64_walls=False):
+                 fp64_walls=False, no_batch=False, drain_below=0):
         if not isinstance(grids, (list, tuple)):
             grids = [grids]
         self.L = _lib.lib()
@@ -182,7 +182,8 @@ class ThermalPlan:
                                    int(mrw_count_trigger), int(max_interactions), deadline,
                                    abort_flag, int(block_threads), int(blocks_per_sm),
                                    int(late_after), int(bool(time_launches)),
-                                   int(mrw_eager_after), int(bool(fp64_walls)))
+                                   int(mrw_eager_after), int(bool(fp64_walls)),
+                                   int(bool(no_batch)), int(drain_below))
         self.timelimit = timelimit
         self._plan = C.c_void_p()
         with torch.cuda.device(self.device):
@@ -321,7 +322,7 @@ def _options(keywords):
         opts["mrw"] = bool(kw.pop("modified_random_walk"))
     for k in ("mrw_gamma", "mrw_tauthres", "mrw_count_trigger", "nepoch", "npilot",
               "max_interactions", "block_threads", "blocks_per_sm", "late_after",
-              "mrw_eager_after", "fp64_walls"):
+              "mrw_eager_after", "fp64_walls", "no_batch", "drain_below"):
         if k in kw:
             opts[k] = kw.pop(k)
     if "timelimit" in kw:

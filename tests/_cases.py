@@ -41,6 +41,9 @@ def case(name):
     if name == "parked":           # packets parked after 40 events, resumed at the end
         m = workloads.small_disk(nr=24, ntheta=24, mass=1e-3, g=0.6)
         return m, dict(late_after=40, mrw=True, mrw_count_trigger=20)
+    if name == "parked_mrw2":      # two species, eager MRW in the resumed walks
+        m = workloads.disk_envelope(nr=20, ntheta=20, mdisk=3e-3, menv=0.01, renv=1000.0)
+        return m, dict(late_after=30, mrw=True, mrw_count_trigger=8, mrw_eager_after=60)
     raise KeyError(name)
 
 

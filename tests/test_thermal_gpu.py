@@ -13,7 +13,7 @@ from tests import _cases
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["disk_full", "disk_mirror", "two_species_mrw", "spiral_3d", "parked"]
+CASES = ["disk_full", "disk_mirror", "two_species_mrw", "spiral_3d", "parked", "parked_mrw2"]
 
 
 def _gpu_run(models, nphot, **kw):
@@ -39,11 +39,12 @@ def test_plain_bit_exact(cuda, name):
               "mrw_steps"):
         assert st[k] == ref["stats"][k], (name, k)
     assert np.array_equal(plan.escape().cpu().numpy()[0], ref["escape"])
-    if name == "parked":
+    if name.startswith("parked"):
         assert st["parked"] > 0 and st["late_units"] > 0
 
 
-@pytest.mark.parametrize("name", ["disk_full", "two_species_mrw", "spiral_3d", "parked"])
+@pytest.mark.parametrize("name", ["disk_full", "two_species_mrw", "spiral_3d", "parked",
+                                  "parked_mrw2"])
 def test_fp64_geometry_bit_exact(cuda, name):
     """The precision-reference instantiation (FP64 positions and walls) against the
     oracle's FP64 geometry."""
@@ -55,6 +56,25 @@ def test_fp64_geometry_bit_exact(cuda, name):
     assert np.array_equal(T, ref["temperature"].reshape(-1)), name
     for k in ("escaped", "killed", "crossings", "events", "mrw_steps"):
         assert st[k] == ref["stats"][k], (name, k)
+
+
+@pytest.mark.parametrize("variant", [dict(no_batch=True), dict(drain_below=-1),
+                                     dict(drain_below=10 ** 9)])
+def test_continuation_schedules_change_nothing(cuda, variant):
+    """Resumed long walks: one per thread, drained to one per warp, in speculative warp
+    batches or one interaction at a time -- the same interactions either way."""
+    models = workloads.walker_models(n=4, seed=8, scale=0.2)
+    kw = dict(seed=4, mrw=True, mrw_count_trigger=10, late_after=60, mrw_eager_after=120)
+    _, E1, T1, s1 = _gpu_run(models, 3000, **kw)
+    _, E2, T2, s2 = _gpu_run(models, 3000, **variant, **kw)
+    assert s1["parked"] > 0
+    if variant.get("drain_below") == 10 ** 9:
+        assert s2["drained"] > 0
+    if variant.get("drain_below") == -1:
+        assert s2["drained"] == 0
+    assert np.array_equal(E1, E2) and np.array_equal(T1, T2)
+    for k in ("events", "crossings", "absorptions", "scatterings", "mrw_steps", "late_units"):
+        assert s1[k] == s2[k], k
 
 
 def test_batched_matches_each_model(cuda):
