@@ -428,6 +428,16 @@ void orc__free_geo(Geo* G) {
  * species; 2 MRW diffusion time, jump cosine, jump azimuth; 3 (n = 0) the emission. */
 enum { RS_EVENT = 0, RS_SECOND = 1, RS_MRW = 2, RS_EMIT = 3 };
 
+/* Upper bound of the distance to the nearest wall, kept along the walk: set from a computed
+ * wall distance D (a lower bound within a relative 5e-6), grown by every move (triangle
+ * inequality, rounded up), unknown after a crossing.  MRW is tried only when the bound
+ * allows a jump. */
+#define ORC_DMAX_UNKNOWN 3.0e38f
+static inline float dmax_of(float D) { return D * 1.00001f; }
+static inline float dmax_after(float dmax, float step) {
+    return dmax < ORC_DMAX_UNKNOWN ? (dmax + step) * 1.000001f : ORC_DMAX_UNKNOWN;
+}
+
 static inline void ev_block(const Pkt* p, uint32_t n, uint32_t stream, float u[4]) {
     uint32_t c[4], o[4];
     c[0] = n; c[1] = p->ctr[1]; c[2] = p->ctr[2]; c[3] = p->ctr[3] | (stream << 24);
@@ -579,16 +589,17 @@ static void rotate_dir(float* kx, float* ky, float* kz, float mu, float cp, floa
     float w2 = 1.0f - az * az;
     if (w2 > 1.0e-10f) {
         float w = sqrtf(w2);
-        nx = mu * ax + st * (ax * az * cp - ay * sp) / w;
-        ny = mu * ay + st * (ay * az * cp + ax * sp) / w;
+        float sw = st / w;
+        nx = mu * ax + sw * (ax * az * cp - ay * sp);
+        ny = mu * ay + sw * (ay * az * cp + ax * sp);
         nz = mu * az - st * cp * w;
     } else {
         nx = st * cp;
         ny = st * sp;
         nz = (az >= 0.0f) ? mu : -mu;
     }
-    float n = sqrtf(nx * nx + ny * ny + nz * nz);
-    *kx = nx / n; *ky = ny / n; *kz = nz / n;
+    float rn = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    *kx = nx * rn; *ky = ny * rn; *kz = nz * rn;
 }
 
 static void iso_dir(Pkt* p, float umu, float uphi) {
@@ -760,6 +771,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         p.tau = -orc_logf(e[3]);
         p.ir = -1; p.itv = 0; p.ip = 0;
         p.last_wall = W_NONE;
+        p.dmax = ORC_DMAX_UNKNOWN;
     }
     for (;;) {
         int c = -1;
@@ -818,21 +830,27 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             cnt->events += 1;
             float ev[4], sb[4];
             ev_block(&p, n, RS_EVENT, ev);
+            p.dmax = dmax_after(p.dmax, (float)se);
             int did_mrw = 0;
-            /* MRW is tried after mrw_count_trigger events in one cell, and at every event
-             * once the packet has made more than mrw_eager_after events (it is trapped).
-             * The wall distance of a try also refreshes the safety distance. */
-            const int tried = o->mrw && (p.cell_events >= o->mrw_count_trigger ||
-                                         (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after));
+            /* MRW is considered after mrw_count_trigger events in one cell, and at every
+             * event once the packet has made more than mrw_eager_after events (it is
+             * trapped).  It is tried (the wall distance computed) only when the distance
+             * bound allows a jump; a try also refreshes the safety distance. */
+            const int cond = o->mrw && (p.cell_events >= o->mrw_count_trigger ||
+                                        (o->mrw_eager_after > 0 && p.nevents > o->mrw_eager_after));
+            int tried = 0;
             float Dw = 0.0f;
+            float aR = 0.0f;
+            if (cond && 0.999f * p.dmax * alpha >= o->mrw_tauthres) {
+                for (int s = 0; s < ns; ++s)
+                    aR = aR + X->rho[(size_t)s * G->ncell + c] *
+                                  row_interp(X, T->kR + (size_t)s * ORC_NROW, s, c);
+                tried = 0.999f * p.dmax * aR >= o->mrw_gamma;
+            }
             if (tried) {
                 Dw = f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p);
                 float R0f = 0.999f * Dw;
                 double R0 = (double)R0f;
-                float aR = 0.0f;
-                for (int s = 0; s < ns; ++s)
-                    aR = aR + X->rho[(size_t)s * G->ncell + c] *
-                                  row_interp(X, T->kR + (size_t)s * ORC_NROW, s, c);
                 if (R0f * aR >= o->mrw_gamma && R0f * alpha >= o->mrw_tauthres) {
                     did_mrw = 1;
                     float mb[4];
@@ -954,9 +972,11 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 p.tau = -orc_logf(ev[1]);
             }
             if (did_mrw || (full && !tried))
-                p.dsafe = 0.999999f * (f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p));
-            else if (tried)
+                Dw = f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p);
+            if (did_mrw || tried || full) {
                 p.dsafe = 0.999999f * Dw;
+                p.dmax = dmax_of(Dw);
+            }
             if (p.nevents >= o->max_interactions) { cnt->killed += 1; return p.nevents; }
             if (X->pilot && X->late_after > 0 && p.nevents >= X->late_after) return p.nevents;
         } else {
@@ -970,6 +990,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             }
             p.tau = p.tau - tcell;
             p.dsafe = 0.0f;
+            p.dmax = ORC_DMAX_UNKNOWN;
             p.ncross += 1;
             cnt->crossings += 1;
             if (X->ccross && c >= 0) atomic_add64(&X->ccross[c], 1);

@@ -115,18 +115,28 @@ __device__ __forceinline__ void mc_rotate(float& kx, float& ky, float& kz, float
     float w2 = 1.0f - az * az;
     if (w2 > 1.0e-10f) {
         float w = sqrtf(w2);
-        nx = mu * ax + st * (ax * az * cp - ay * sp) / w;
-        ny = mu * ay + st * (ay * az * cp + ax * sp) / w;
+        float sw = st / w;
+        nx = mu * ax + sw * (ax * az * cp - ay * sp);
+        ny = mu * ay + sw * (ay * az * cp + ax * sp);
         nz = mu * az - st * cp * w;
     } else {
         nx = st * cp;
         ny = st * sp;
         nz = (az >= 0.0f) ? mu : -mu;
     }
-    float n = sqrtf(nx * nx + ny * ny + nz * nz);
-    kx = nx / n;
-    ky = ny / n;
-    kz = nz / n;
+    float rn = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    kx = nx * rn;
+    ky = ny * rn;
+    kz = nz * rn;
+}
+
+// Upper bound of the distance to the nearest wall of the cell, kept along the walk: set
+// from a computed wall distance D (which is a lower bound within a relative 5e-6), grown
+// by every move (triangle inequality, rounded up), unknown after a crossing.
+#define MC_DMAX_UNKNOWN 3.0e38f
+__device__ __forceinline__ float mc_dmax_of(float D) { return D * 1.00001f; }
+__device__ __forceinline__ float mc_dmax_after(float dmax, float step) {
+    return dmax < MC_DMAX_UNKNOWN ? (dmax + step) * 1.000001f : MC_DMAX_UNKNOWN;
 }
 
 // Smallest index l with cdf[l] > u (cdf[n-1] == 1 > u).

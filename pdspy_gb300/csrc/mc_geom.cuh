@@ -20,6 +20,7 @@ enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI
 struct Pkt {
     double x, y, z;
     float dsafe;    // lower bound of the distance to every wall of the cell
+    float dmax;     // upper bound of the distance to the nearest wall (3e38: unknown)
     float kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events;

@@ -82,6 +82,7 @@ __device__ __forceinline__ ds ds_move2(ds a, ds s, float k) {
 struct PktS {
     ds x, y, z;
     float dsafe;    // lower bound of the distance to every wall of the cell
+    float dmax;     // upper bound of the distance to the nearest wall (3e38: unknown)
     float kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events;

@@ -58,7 +58,7 @@ struct __align__(16) ParkRec {
     int ir, itv, ip, lam;
     int last_wall, cell_events, nevents, ncross;
     int m, epoch;
-    uint32_t pid, model, tag, spare;
+    uint32_t pid, model, tag, spare;   // spare: bits of dmax
     int pad[3];
 };
 
@@ -354,6 +354,7 @@ __device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, cons
     p.tau = -mc_logf(mc_u01(e.w));
     G::origin(p);
     p.dsafe = 0.0f;
+    p.dmax = MC_DMAX_UNKNOWN;
     p.ir = -1; p.itv = 0; p.ip = 0;
     p.last_wall = W_NONE;
     p.cell_events = 0;
@@ -369,7 +370,8 @@ __device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p) 
     r.ir = p.ir; r.itv = p.itv; r.ip = p.ip; r.lam = p.lam;
     r.last_wall = p.last_wall; r.cell_events = p.cell_events;
     r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
-    r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag; r.spare = 0;
+    r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag;
+    r.spare = __float_as_uint(p.dmax);
     r.pad[0] = 0; r.pad[1] = 0; r.pad[2] = 0;
 }
 
@@ -382,6 +384,7 @@ __device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r) 
     p.last_wall = r.last_wall; p.cell_events = r.cell_events;
     p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
     p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag;
+    p.dmax = __uint_as_float(r.spare);
 }
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
@@ -439,24 +442,30 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         int64_t* dep = late ? P.Elate : P.E;
         const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
         const uint4 ev = mc_block(p.rng, n, MC_RS_EVENT, k0, k1);
+        p.dmax = mc_dmax_after(p.dmax, G::f(se));
         bool did_mrw = false;
-        // MRW is tried after mrw_count_trigger events in one cell, and at every event once
-        // the packet has made more than mrw_eager_after events (it is trapped).  The wall
-        // distance of a try also refreshes the safety distance.
-        const bool tried = P.mrw && (p.cell_events >= P.mrw_trigger ||
-                                     (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after));
+        // MRW is considered after mrw_count_trigger events in one cell, and at every event
+        // once the packet has made more than mrw_eager_after events (it is trapped).  It is
+        // tried (the wall distance computed) only when the upper bound of that distance
+        // allows a jump; a try also refreshes the safety distance.
+        const bool cond = P.mrw && (p.cell_events >= P.mrw_trigger ||
+                                    (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after));
+        bool tried = false;
         float Dw = 0.0f;
-        if (tried) {
-            Dw = G::dist(M, dp, P.fpool, p);
-            float R0f = 0.999f * Dw;
-            len_t R0 = G::of(R0f);
-            float2 qv[NS];
-            float aR = 0.0f;
+        float2 qv[NS];
+        float aR = 0.0f;
+        if (cond && 0.999f * p.dmax * alpha >= P.mrw_tauthres) {
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
                 qv[s] = qa[base + (int64_t)s * M.ncell + c];
                 aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
             }
+            tried = 0.999f * p.dmax * aR >= P.mrw_gamma;
+        }
+        if (tried) {
+            Dw = G::dist(M, dp, P.fpool, p);
+            float R0f = 0.999f * Dw;
+            len_t R0 = G::of(R0f);
             if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
                 did_mrw = true;
                 const uint4 mb = mc_block(p.rng, n, MC_RS_MRW, k0, k1);
@@ -582,9 +591,11 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
             }
             p.tau = -mc_logf(mc_u01(ev.y));
         }
-        if (did_mrw) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
-        else if (tried) p.dsafe = 0.999999f * Dw;
-        else if (full) p.dsafe = 0.999999f * G::dist(M, dp, P.fpool, p);
+        if (did_mrw || (full && !tried)) Dw = G::dist(M, dp, P.fpool, p);
+        if (did_mrw || tried || full) {
+            p.dsafe = 0.999999f * Dw;
+            p.dmax = mc_dmax_of(Dw);
+        }
         if (late) cnt.late += 1;
         if (p.nevents >= P.max_inter) {
             cnt.killed += 1;
@@ -606,6 +617,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     G::move(p, sw, p.kx, p.ky, p.kz);
     p.tau = p.tau - tcell;
     p.dsafe = 0.0f;
+    p.dmax = MC_DMAX_UNKNOWN;
     p.ncross += 1;
     cnt.crossings += 1;
     p.cell_events = 0;
@@ -667,7 +679,7 @@ __device__ __forceinline__ S shfl_struct(const S& v, int src) {
 // does not allow a batch.
 template <int NS, class G>
 __device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt,
-                         int lane, bool* cut) {
+                         int lane, int bmax, bool* cut) {
     using Pk = typename G::Pkt;
     using len_t = typename G::len_t;
     const unsigned FULL = 0xffffffffu;
@@ -677,7 +689,7 @@ __device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& 
     const double* __restrict__ dp = P.dpool;
     const int nl = P.nl;
     const uint32_t k0 = P.key0, k1 = P.key1;
-    int B = 32;
+    int B = bmax < 32 ? bmax : 32;
     const long long room = (long long)P.max_inter - 1 - (long long)p.nevents;
     if (room < (long long)B) B = room > 0 ? (int)room : 0;
     if (B <= 0) return -1;
@@ -796,32 +808,39 @@ __device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& 
         if (lane == j) post = q;
     }
     if (B <= 0) return -1;
-    // phase 3: wall distance after each interaction and the MRW test
+    // phase 3: wall distance after each interaction
     float D = 0.0f;
-    bool tried = false, ok = false;
-    if (lane < B) {
-        tried = P.mrw && (post.cell_events >= P.mrw_trigger ||
-                          (P.mrw_eager_after > 0 && post.nevents > P.mrw_eager_after));
-        D = G::dist(M, dp, P.fpool, post);
-        const float R0f = 0.999f * D;
-        ok = tried && (R0f * aR >= P.mrw_gamma && R0f * my_alpha >= P.mrw_tauthres);
-    }
-    const unsigned live = (B >= 32) ? FULL : ((1u << B) - 1u);
-    const unsigned okm = __ballot_sync(FULL, ok) & live;
-    const int Jm = okm ? (__ffs(okm) - 1) : B;   // first MRW jump
-    // phase 4: safety-distance replay (which interactions need a wall solve)
-    float dsf = p.dsafe;
+    if (lane < B) D = G::dist(M, dp, P.fpool, post);
+    // phase 4: replay of the safety distance, the distance bound and the MRW decisions
+    float dsf = p.dsafe, dmx = p.dmax;
+    int Jm = B;   // first MRW jump
     bool my_full = false;
-    float my_dsafe = 0.0f;
-    const int Jr = Jm < B ? Jm + 1 : B;
-    for (int j = 0; j < Jr; ++j) {
+    float my_dsafe = 0.0f, my_dmax = 0.0f;
+    for (int j = 0; j < B; ++j) {
         const float sef_j = __shfl_sync(FULL, my_sef, j);
         const float D_j = __shfl_sync(FULL, D, j);
-        const bool tr_j = __shfl_sync(FULL, tried, j);
+        const float a_j = __shfl_sync(FULL, my_alpha, j);
+        const int ce_j = p.cell_events + j + 1;
+        const int nv_j = p.nevents + j + 1;
         const bool full = !(sef_j < dsf);
-        dsf = (full || tr_j) ? 0.999999f * D_j : dsf - sef_j;
-        if (lane == j) { my_full = full; my_dsafe = dsf; }
+        dmx = mc_dmax_after(dmx, sef_j);
+        const bool cond = P.mrw && (ce_j >= P.mrw_trigger ||
+                                    (P.mrw_eager_after > 0 && nv_j > P.mrw_eager_after));
+        bool tried = false;
+        if (cond && 0.999f * dmx * a_j >= P.mrw_tauthres) tried = 0.999f * dmx * aR >= P.mrw_gamma;
+        const float R0f = 0.999f * D_j;
+        if (lane == j) my_full = full;
+        if (tried && R0f * aR >= P.mrw_gamma && R0f * a_j >= P.mrw_tauthres) { Jm = j; break; }
+        if (full || tried) {
+            dsf = 0.999999f * D_j;
+            dmx = mc_dmax_of(D_j);
+        } else {
+            dsf = dsf - sef_j;
+        }
+        if (lane == j) { my_dsafe = dsf; my_dmax = dmx; }
     }
+    const unsigned live = (B >= 32) ? FULL : ((1u << B) - 1u);
+    const int Jr = Jm < B ? Jm + 1 : B;
     // phase 5: wall solves of the interactions the safety distance did not clear
     bool bad = false;
     if (lane < Jr && my_full) {
@@ -853,6 +872,7 @@ __device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& 
         if (J > 0) {
             p = shfl_struct(post, J - 1);
             p.dsafe = __shfl_sync(FULL, my_dsafe, J - 1);
+            p.dmax = __shfl_sync(FULL, my_dmax, J - 1);
         }
         return J;
     }
@@ -916,7 +936,9 @@ __device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& 
         m.lam = lsel;
         m.tau = tn;
         m.cell_events = 0;
-        m.dsafe = 0.999999f * G::dist(M, dp, P.fpool, m);
+        const float D2 = G::dist(M, dp, P.fpool, m);
+        m.dsafe = 0.999999f * D2;
+        m.dmax = mc_dmax_of(D2);
     }
     p = shfl_struct(m, Jm);
     cnt.events += 1;
@@ -1132,9 +1154,16 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         park_load<G>(p, P.park_in[g]);
         WarpPol pol(lane);
         bool alive = true;
+        // batch length follows the recent run length between interruptions (a batch planned
+        // much longer only adds sequential work that is thrown away)
+        float run = 8.0f;
         while (alive) {
             bool cut = true;
-            if (P.batch) seb_batch<NS, G>(p, P, T, cnt, lane, &cut);
+            if (P.batch) {
+                const int bmax = min(32, max(4, (int)(2.0f * run) + 2));
+                const int got = seb_batch<NS, G>(p, P, T, cnt, lane, bmax, &cut);
+                if (got >= 0) run = 0.75f * run + 0.25f * (float)got;
+            }
             if (cut) alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
