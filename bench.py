@@ -8,12 +8,15 @@ ntheta 64..192), small-grain dust with HG scattering, modified random walk on wi
 pdspy's production settings (gamma 2, tauthres 10, count trigger 100).  Synthetic
 inputs, built in memory.
 
-A step is one full thermal run of the batch (all epochs, the continuation launch and the
-temperature inversion).  ``value`` is packets/s with densities resident in HBM; ``e2e`` is
-the same through the public API with host arrays: pinned H2D of the densities, the run,
-D2H of the temperatures.  The reference arm (``--impl reference``) times the CPU
-restatement of the same algorithm (the reference's own path is the external RADMC-3D
-binary, which is not available) on a bounded sample of the workload.
+A step is one full thermal run of the batch (all epochs, both continuation stages and the
+temperature inversion).  ``value`` is packets/s with the densities resident in HBM (CUDA
+events around the run); ``e2e`` is the same step through the public API with host arrays,
+timed on the same stream from the pinned H2D copy of the densities to the D2H copy of the
+temperatures.  The longest packet walk of this workload (about 1e8 interactions for one
+walker at 1e6 packets) sets most of a step's time, so the default is one timed step and
+warm-up runs are cut at a short device deadline.  The reference arm (``--impl reference``)
+times the CPU restatement of the same algorithm (the reference's own path is the external
+RADMC-3D binary, which is not available) on a bounded sample of the workload.
 
 With torchrun (N > 1) every rank runs its own independent batch of walkers (the models
 shard with no data-path collective): weak scaling, value = all ranks' packets / max time.
@@ -38,7 +41,7 @@ METRIC = "packets/s batched vs plain GPU at <=1% median dT/T; adjoint grads/s; h
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "plain"],
@@ -46,12 +49,13 @@ def parse():
     ap.add_argument("--models", type=int, default=64)
     ap.add_argument("--packets", type=int, default=1000000, help="packets per model")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-models", type=int, default=8)
     ap.add_argument("--cpu-packets", type=int, default=100000)
-    ap.add_argument("--timelimit", type=float, default=600.0,
-                    help="device-side deadline per thermal run (s)")
+    ap.add_argument("--timelimit", type=float, default=1800.0,
+                    help="device-side deadline per timed thermal run (s)")
+    ap.add_argument("--warmup-deadline", type=float, default=10.0,
+                    help="device-side deadline of each warm-up run (s)")
     return ap.parse_args()
 
 
@@ -198,57 +202,51 @@ def main():
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    # Warm-up: the same plan and kernels, each run cut at a short device deadline (the
+    # longest packet walk of this workload alone takes minutes; warm-up only has to load
+    # the modules and settle clocks and caches).
+    plan.set_timelimit(args.warmup_deadline)
     for _ in range(args.warmup):
         plan.run(rho, T)
-    plan.check_status()
+        torch.cuda.synchronize(dev)
+    plan.set_timelimit(args.timelimit)
 
-    # device-resident timing
-    step_ms, launch_ms, stats = [], [], []
+    # Timed steps.  Per step, on the run's stream: event a, pinned host -> device copy of the
+    # densities, event b, the thermal run, event c, device -> pinned host copy of the
+    # temperatures, event d.  value uses b..c (inputs resident in HBM), e2e uses a..d.
+    step_ms, e2e_ms, launch_ms, launch_stats, stats = [], [], [], [], []
     with Clocks(local) as clk:
         for _ in range(args.steps):
             flush.zero_()
             barrier()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            plan.run(rho, T)
-            b.record(stream)
-            barrier()
-            step_ms.append(a.elapsed_time(b))
-            launch_ms.append(plan.launch_ms())
-            stats.append(plan.check_status())
-    t_local = float(np.sum(step_ms))
-    t_max = t_local
-    if world > 1:
-        tt = torch.tensor([t_local], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * total_packets * args.steps / (t_max / 1e3)
-
-    # end to end through the public API with host buffers
-    e2e = None
-    if not args.no_e2e:
-        e_ms = []
-        for i in range(args.steps):
-            flush.zero_()
-            barrier()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
             rho.copy_(host_rho, non_blocking=True)
+            ev[1].record(stream)
             plan.run(rho, T)
+            ev[2].record(stream)
             host_T.copy_(T, non_blocking=True)
-            b.record(stream)
+            ev[3].record(stream)
             barrier()
-            e_ms.append(a.elapsed_time(b))
-        te = float(np.sum(e_ms))
+            step_ms.append(ev[1].elapsed_time(ev[2]))
+            e2e_ms.append(ev[0].elapsed_time(ev[3]))
+            launch_ms.append(plan.launch_ms())
+            launch_stats.append(plan.launch_stats())
+            stats.append(plan.check_status())
+
+    def max_over_ranks(v):
         if world > 1:
-            tt = torch.tensor([te], device=dev)
+            tt = torch.tensor([v], device=dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        e2e = {"value": world * total_packets * args.steps / (te / 1e3), "unit": "packets/s",
-               "h2d_bytes_per_step": int(host_rho.numel() * 4),
-               "d2h_bytes_per_step": int(host_T.numel() * 8)}
+            return float(tt.item())
+        return v
+
+    t_max = max_over_ranks(float(np.sum(step_ms)))
+    te = max_over_ranks(float(np.sum(e2e_ms)))
+    value = world * total_packets * args.steps / (t_max / 1e3)
+    e2e = {"value": world * total_packets * args.steps / (te / 1e3), "unit": "packets/s",
+           "h2d_bytes_per_step": int(host_rho.numel() * 4),
+           "d2h_bytes_per_step": int(host_T.numel() * 8)}
 
     # roofline of the dominant kernel (the transport launches)
     peaks = {}
@@ -286,22 +284,28 @@ def main():
                (args.cpu_models, args.cpu_packets, dt)}
 
     K, P = plan.opts.nepoch, plan.opts.npilot
-    launches_per_step = 2 * (st["launches"]) - 1 + 3
+    # start + (prep + transport) per pass and epoch + two continuation launches +
+    # temperature + finish
+    launches_per_step = 2 * st["launches"] + 1
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": workload_name(args), "models_per_gpu": args.models,
                            "packets_per_model": args.packets, "mrw": True, "nepoch": K,
                            "npilot": P, "late_after": int(plan.opts.late_after),
                            "l2": "256 MB buffer written between timed steps",
+                           "warmup": "same plan, each run cut at a %g s device deadline" %
+                                     args.warmup_deadline,
+                           "geometry": "double-single (FP32 pipe); FP64 energy->temperature",
                            "parallelism": "replicas: independent walker batches per GPU"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
-                                            "parked", "killed")},
-                "launch_ms": [round(x, 3) for x in launch_ms[-1]]}
+                                            "parked", "drained", "killed", "late_units")},
+                "launch_ms": [round(x, 3) for x in launch_ms[-1]],
+                "launch_longest_walk": [b for (_, b, _) in launch_stats[-1]]}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

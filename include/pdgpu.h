@@ -172,6 +172,10 @@ pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* plan, const float* rho, double* te
  * run when options.time_launches was set; returns the number written (<= capacity). */
 int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* plan, float* ms, int32_t capacity);
 
+/* Device-clock budget of the plan's later runs (ns, 0 = none); the timelimit argument of
+ * radmc3d.run.thermal (radmc3d/run.py:9-38) per run instead of per plan. */
+pdgpu_status pdgpu_mc_plan_set_deadline(pdgpu_mc_plan* plan, int64_t deadline_ns);
+
 pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* plan, const void* workspace, void* stream,
                                  pdgpu_mc_stats* stats);
 

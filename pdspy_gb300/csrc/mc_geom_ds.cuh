@@ -386,4 +386,52 @@ __device__ inline float wall_distance_ds(const McModel& M, const WallsS& W, cons
     return m > 0.0f ? m : 0.0f;
 }
 
+// The same lower bound computed by a whole warp, one wall per lane (0 inner sphere, 1 outer
+// sphere, 2-3 cones, 4-5 phi half-planes) and reduced with min, which gives exactly the
+// value of wall_distance_ds.  Every lane returns the result.
+__device__ inline float wall_distance_ds_warp(const McModel& M, const WallsS& W, const PktS& p,
+                                              int lane) {
+    float d = 3.0e38f;
+    if (lane < 6) {
+        ds x2 = ds_sqr(p.x), y2 = ds_sqr(p.y), z2 = ds_sqr(p.z);
+        ds rho2 = ds_add(x2, y2);
+        ds r2 = ds_add(rho2, z2);
+        if (lane < 2) {
+            float rf = sqrtf(r2.h);
+            if (lane == 0) d = ds_sub(r2, W.R2(p.ir)).h / (rf + W.RH[p.ir]);
+            else d = ds_sub(W.R2(p.ir + 1), r2).h / (rf + W.RH[p.ir + 1]);
+        } else if (lane < 4) {
+            int w = p.itv + (lane - 2);
+            if (w != 0 && w != M.ntv) {
+                float rhof = sqrtf(rho2.h);
+                float a = rhof * W.MU[w];
+                float b = p.z.h * W.SN[w];
+                if ((a > 0.0f) == (b > 0.0f)) {
+                    float num = ds_sub(ds_mul(W.MU2(w), r2), z2).h;
+                    float den = fabsf(a) + fabsf(b);
+                    d = den > 0.0f ? fabsf(num) / den : 0.0f;
+                } else {
+                    d = fabsf(a) + fabsf(b);
+                }
+            }
+        } else if (M.np > 1) {
+            if (lane == 4) {
+                int k0 = p.ip;
+                d = fabsf(ds_add(ds_mulf(p.x, -W.SP[k0]), ds_mulf(p.y, W.CP[k0])).h);
+            } else {
+                int k1 = p.ip + 1;
+                d = fabsf(ds_add(ds_mulf(p.x, W.SP[k1]), ds_mulf(p.y, -W.CP[k1])).h);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        float e = __shfl_xor_sync(0xffffffffu, d, o);
+        if (e < d) d = e;
+    }
+    d = __shfl_sync(0xffffffffu, d, 0);
+    float m = d * (1.0f - 4.0e-6f);
+    return m > 0.0f ? m : 0.0f;
+}
+
 }  // namespace pdgpu

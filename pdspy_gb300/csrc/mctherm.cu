@@ -168,6 +168,11 @@ struct GeoS {
         WallsS W(M, fp);
         return wall_distance_ds(M, W, p);
     }
+    static __device__ __forceinline__ float dist_warp(int lane, const McModel& M, const double*,
+                                                      const float* fp, const Pkt& p) {
+        WallsS W(M, fp);
+        return wall_distance_ds_warp(M, W, p, lane);
+    }
     static __device__ __forceinline__ void locate(const McModel& M, const double*, const float* fp,
                                                   Pkt& p) {
         WallsS W(M, fp);
@@ -232,6 +237,10 @@ struct GeoD {
                                                  const Pkt& p) {
         return wall_distance(M, dp, fp, p);
     }
+    static __device__ __forceinline__ float dist_warp(int, const McModel& M, const double* dp,
+                                                      const float* fp, const Pkt& p) {
+        return wall_distance(M, dp, fp, p);
+    }
     static __device__ __forceinline__ void locate(const McModel& M, const double* dp, const float*,
                                                   Pkt& p) {
         locate_angles(M, dp, p);
@@ -254,13 +263,47 @@ struct GeoD {
     }
 };
 
+// Uniforms (and the quantities derived from them alone) of one interaction, by stream.
+struct EvR {
+    float ua, tn, umu, cs, sn;   // albedo test, new optical depth, cosine, azimuth sin/cos
+};
+struct SecR {
+    float uq, urow, ucdf, us;    // reemission q', row and CDF picks, species pick
+};
+struct MrwR {
+    float uy, jmu, jcs, jsn;     // diffusion time, jump cosine and azimuth
+};
+
+__device__ __forceinline__ EvR ev_of(uint4 b) {
+    EvR r;
+    r.ua = mc_u01(b.x);
+    r.tn = -mc_logf(mc_u01(b.y));
+    r.umu = mc_u01(b.z);
+    mc_sincospif2(mc_u01(b.w), r.sn, r.cs);
+    return r;
+}
+__device__ __forceinline__ SecR sec_of(uint4 b) {
+    SecR r;
+    r.uq = mc_u01(b.x); r.urow = mc_u01(b.y); r.ucdf = mc_u01(b.z); r.us = mc_u01(b.w);
+    return r;
+}
+__device__ __forceinline__ MrwR mrw_of(uint4 b) {
+    MrwR r;
+    r.uy = mc_u01(b.x);
+    r.jmu = 2.0f * mc_u01(b.y) - 1.0f;
+    mc_sincospif2(mc_u01(b.z), r.jsn, r.jcs);
+    return r;
+}
+
 // Execution policies of the transport step.
 //
-// LanePol: one packet per thread (the epoch launches).
-// WarpPol: one packet per warp, its state replicated in all 32 lanes (the continuation of
-// long parked packets, whose sequential chains set the run time).  The lanes share the
-// work that is independent within a step: table searches count the entries <= the key
-// with ballots, and the wall candidates are solved on separate lanes.  Every result is
+// LanePol: one packet per thread (the epoch launches and the first continuation stage).
+// WarpPol: one packet per warp, its state replicated in all 32 lanes (the last, longest
+// walks, whose sequential chains set the run time), organised for latency: the random
+// numbers of the next 32 interactions are drawn at once (lane l holds interaction n0 + l,
+// an interaction reads its values with shuffles), the cell's Rosseland and Planck means
+// are kept while the packet stays in the cell, table searches count entries with ballots,
+// and wall candidates and wall distances are computed one wall per lane.  Every result is
 // identical to the per-thread code; memory side effects are issued by lane 0.
 struct LanePol {
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
@@ -275,12 +318,40 @@ struct LanePol {
                                                       int& w) const {
         return G::wall_lane(M, dp, fp, p, w);
     }
+    template <class G>
+    __device__ __forceinline__ float dist(const McModel& M, const double* dp, const float* fp,
+                                          const typename G::Pkt& p) const {
+        return G::dist(M, dp, fp, p);
+    }
+    __device__ __forceinline__ EvR ev(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        return ev_of(mc_block(r, n, MC_RS_EVENT, k0, k1));
+    }
+    __device__ __forceinline__ SecR second(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        return sec_of(mc_block(r, n, MC_RS_SECOND, k0, k1));
+    }
+    __device__ __forceinline__ MrwR mrwd(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        return mrw_of(mc_block(r, n, MC_RS_MRW, k0, k1));
+    }
+    __device__ __forceinline__ bool cached(int, int, int, int) const { return false; }
+    __device__ __forceinline__ void remember(int, int, int, int, float) {}
+    __device__ __forceinline__ float cached_value(int) const { return 0.0f; }
     __device__ __forceinline__ bool leader() const { return true; }
 };
 
 struct WarpPol {
     int lane;
-    __device__ __forceinline__ explicit WarpPol(int l) : lane(l) {}
+    // random numbers of interactions n0 .. n0 + 31, lane l holding n0 + l
+    bool rv;
+    uint32_t n0;
+    EvR re;
+    SecR rs;
+    MrwR rm;
+    // per-cell cache: (model, cell, epoch) -> values by slot (Rosseland, Planck per species)
+    int cm, cc, ce;
+    unsigned cvalid;
+    float cval[1 + MC_MAX_SPEC];
+    __device__ __forceinline__ explicit WarpPol(int l)
+        : lane(l), rv(false), n0(0), cm(-1), cc(-1), ce(-1), cvalid(0u) {}
     // number of entries <= u of a non-decreasing table == smallest index with c > u
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
         int cnt = 0;
@@ -314,6 +385,59 @@ struct WarpPol {
                                                       int& w) const {
         return G::wall_warp(lane, M, dp, fp, p, w);
     }
+    template <class G>
+    __device__ __forceinline__ float dist(const McModel& M, const double* dp, const float* fp,
+                                          const typename G::Pkt& p) const {
+        return G::dist_warp(lane, M, dp, fp, p);
+    }
+    __device__ __forceinline__ int slot(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        if (!rv || n < n0 || n - n0 >= 32u) {
+            n0 = n;
+            const uint32_t m = n + (uint32_t)lane;
+            re = ev_of(mc_block(r, m, MC_RS_EVENT, k0, k1));
+            rs = sec_of(mc_block(r, m, MC_RS_SECOND, k0, k1));
+            rm = mrw_of(mc_block(r, m, MC_RS_MRW, k0, k1));
+            rv = true;
+        }
+        return (int)(n - n0);
+    }
+    __device__ __forceinline__ EvR ev(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        const int l = slot(r, n, k0, k1);
+        EvR o;
+        o.ua = __shfl_sync(0xffffffffu, re.ua, l);
+        o.tn = __shfl_sync(0xffffffffu, re.tn, l);
+        o.umu = __shfl_sync(0xffffffffu, re.umu, l);
+        o.cs = __shfl_sync(0xffffffffu, re.cs, l);
+        o.sn = __shfl_sync(0xffffffffu, re.sn, l);
+        return o;
+    }
+    __device__ __forceinline__ SecR second(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        const int l = slot(r, n, k0, k1);
+        SecR o;
+        o.uq = __shfl_sync(0xffffffffu, rs.uq, l);
+        o.urow = __shfl_sync(0xffffffffu, rs.urow, l);
+        o.ucdf = __shfl_sync(0xffffffffu, rs.ucdf, l);
+        o.us = __shfl_sync(0xffffffffu, rs.us, l);
+        return o;
+    }
+    __device__ __forceinline__ MrwR mrwd(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        const int l = slot(r, n, k0, k1);
+        MrwR o;
+        o.uy = __shfl_sync(0xffffffffu, rm.uy, l);
+        o.jmu = __shfl_sync(0xffffffffu, rm.jmu, l);
+        o.jcs = __shfl_sync(0xffffffffu, rm.jcs, l);
+        o.jsn = __shfl_sync(0xffffffffu, rm.jsn, l);
+        return o;
+    }
+    __device__ __forceinline__ bool cached(int m, int c, int e, int k) const {
+        return cm == m && cc == c && ce == e && ((cvalid >> k) & 1u);
+    }
+    __device__ __forceinline__ void remember(int m, int c, int e, int k, float v) {
+        if (cm != m || cc != c || ce != e) { cm = m; cc = c; ce = e; cvalid = 0u; }
+        cval[k] = v;
+        cvalid |= 1u << k;
+    }
+    __device__ __forceinline__ float cached_value(int k) const { return cval[k]; }
     __device__ __forceinline__ bool leader() const { return lane == 0; }
 };
 
@@ -441,7 +565,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         const bool late = P.late_after > 0 && p.nevents > P.late_after;
         int64_t* dep = late ? P.Elate : P.E;
         const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
-        const uint4 ev = mc_block(p.rng, n, MC_RS_EVENT, k0, k1);
+        const EvR ev = pol.ev(p.rng, n, k0, k1);
         p.dmax = mc_dmax_after(p.dmax, G::f(se));
         bool did_mrw = false;
         // MRW is considered after mrw_count_trigger events in one cell, and at every event
@@ -456,21 +580,26 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         float aR = 0.0f;
         if (cond && 0.999f * p.dmax * alpha >= P.mrw_tauthres) {
 #pragma unroll
-            for (int s = 0; s < NS; ++s) {
-                qv[s] = qa[base + (int64_t)s * M.ncell + c];
-                aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+            for (int s = 0; s < NS; ++s) qv[s] = qa[base + (int64_t)s * M.ncell + c];
+            if (pol.cached(p.m, c, p.epoch, 0)) {
+                aR = pol.cached_value(0);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+                    aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                pol.remember(p.m, c, p.epoch, 0, aR);
             }
             tried = 0.999f * p.dmax * aR >= P.mrw_gamma;
         }
         if (tried) {
-            Dw = G::dist(M, dp, P.fpool, p);
+            Dw = pol.template dist<G>(M, dp, P.fpool, p);
             float R0f = 0.999f * Dw;
             len_t R0 = G::of(R0f);
             if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
                 did_mrw = true;
-                const uint4 mb = mc_block(p.rng, n, MC_RS_MRW, k0, k1);
-                const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
-                float uy = mc_u01(mb.x);
+                const MrwR mb = pol.mrwd(p.rng, n, k0, k1);
+                const SecR sb = pol.second(p.rng, n, k0, k1);
+                float uy = mb.uy;
                 float f = uy * (float)(MC_NMRW - 1);
                 int i = (int)f;
                 if (i > MC_NMRW - 2) i = MC_NMRW - 2;
@@ -481,7 +610,12 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 float aP = 0.0f;
 #pragma unroll
                 for (int s = 0; s < NS; ++s) {
-                    kp[s] = rh[s] * row_interp(pol, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                    if (pol.cached(p.m, c, p.epoch, 1 + s)) {
+                        kp[s] = pol.cached_value(1 + s);
+                    } else {
+                        kp[s] = rh[s] * row_interp(pol, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
+                        pol.remember(p.m, c, p.epoch, 1 + s, kp[s]);
+                    }
                     aP = aP + kp[s];
                     float units_f = kp[s] * ell * 1048576.0f + 0.5f;
                     if (units_f > 9.0e18f) units_f = 9.0e18f;
@@ -492,24 +626,20 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 float dx, dy, dz;
                 {
-                    float mu = 2.0f * mc_u01(mb.y) - 1.0f;
-                    float sn, cs;
-                    mc_sincospif2(mc_u01(mb.z), sn, cs);
+                    float mu = mb.jmu;
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
-                    dx = st * cs; dy = st * sn; dz = mu;
+                    dx = st * mb.jcs; dy = st * mb.jsn; dz = mu;
                 }
                 G::move(p, R0, dx, dy, dz);
                 {
-                    float mu = sqrtf(mc_u01(ev.z));
-                    float sn, cs;
-                    mc_sincospif2(mc_u01(ev.w), sn, cs);
+                    float mu = sqrtf(ev.umu);
                     float kx = dx, ky = dy, kz = dz;
-                    mc_rotate(kx, ky, kz, mu, cs, sn);
+                    mc_rotate(kx, ky, kz, mu, ev.cs, ev.sn);
                     p.kx = kx; p.ky = ky; p.kz = kz;
                 }
                 int sp = 0;
                 if (NS > 1) {
-                    float us = mc_u01(sb.w) * aP;
+                    float us = sb.us * aP;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -522,22 +652,22 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
 #pragma unroll
                 for (int s = 1; s < NS; ++s)
                     if (s == sp) qs = qv[s];
-                p.lam = reemit_lambda(pol, T, nl, qs, sp, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
-                p.tau = -mc_logf(mc_u01(ev.y));
+                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf);
+                p.tau = ev.tn;
                 p.cell_events = 0;
                 cnt.mrw += 1;
             }
         }
         if (!did_mrw) {
-            float ua = mc_u01(ev.x);
+            float ua = ev.ua;
             float asca = 0.0f;
 #pragma unroll
             for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + p.lam];
             if (ua * alpha < asca) {
                 int sp = 0;
                 if (NS > 1) {
-                    const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
-                    float us = mc_u01(sb.w) * asca;
+                    const SecR sb = pol.second(p.rng, n, k0, k1);
+                    float us = sb.us * asca;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -547,7 +677,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                     }
                 }
                 float g = T.g[sp * nl + p.lam];
-                float umu = mc_u01(ev.z);
+                float umu = ev.umu;
                 float mu;
                 if (fabsf(g) < 1.0e-4f) {
                     mu = 2.0f * umu - 1.0f;
@@ -557,18 +687,16 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                     if (mu < -1.0f) mu = -1.0f;
                     if (mu > 1.0f) mu = 1.0f;
                 }
-                float sn, cs;
-                mc_sincospif2(mc_u01(ev.w), sn, cs);
-                mc_rotate(p.kx, p.ky, p.kz, mu, cs, sn);
+                mc_rotate(p.kx, p.ky, p.kz, mu, ev.cs, ev.sn);
                 cnt.scatter += 1;
             } else {
-                const uint4 sb = mc_block(p.rng, n, MC_RS_SECOND, k0, k1);
+                const SecR sb = pol.second(p.rng, n, k0, k1);
                 int sp = 0;
                 if (NS > 1) {
                     float aabs = 0.0f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + p.lam];
-                    float us = mc_u01(sb.w) * aabs;
+                    float us = sb.us * aabs;
                     float acc = 0.0f;
                     sp = NS - 1;
 #pragma unroll
@@ -579,19 +707,17 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
-                p.lam = reemit_lambda(pol, T, nl, qa[idx], sp, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
+                p.lam = reemit_lambda(pol, T, nl, qa[idx], sp, sb.uq, sb.urow, sb.ucdf);
                 {
-                    float mu = 2.0f * mc_u01(ev.z) - 1.0f;
-                    float sn, cs;
-                    mc_sincospif2(mc_u01(ev.w), sn, cs);
+                    float mu = 2.0f * ev.umu - 1.0f;
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
-                    p.kx = st * cs; p.ky = st * sn; p.kz = mu;
+                    p.kx = st * ev.cs; p.ky = st * ev.sn; p.kz = mu;
                 }
                 cnt.absorb += 1;
             }
-            p.tau = -mc_logf(mc_u01(ev.y));
+            p.tau = ev.tn;
         }
-        if (did_mrw || (full && !tried)) Dw = G::dist(M, dp, P.fpool, p);
+        if (did_mrw || (full && !tried)) Dw = pol.template dist<G>(M, dp, P.fpool, p);
         if (did_mrw || tried || full) {
             p.dsafe = 0.999999f * Dw;
             p.dmax = mc_dmax_of(Dw);
@@ -1656,6 +1782,12 @@ int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* P, float* ms, int32_t capacity) {
         ms[i] = t;
     }
     return n;
+}
+
+pdgpu_status pdgpu_mc_plan_set_deadline(pdgpu_mc_plan* P, int64_t deadline_ns) {
+    if (!P || deadline_ns < 0) return PDGPU_INVALID_ARG;
+    P->opt.deadline_ns = deadline_ns;
+    return PDGPU_OK;
 }
 
 pdgpu_status pdgpu_mc_plan_layout(const pdgpu_mc_plan* P, pdgpu_mc_layout* L) {

@@ -246,6 +246,12 @@ class ThermalPlan:
                 out.append(((t1 - t0) / 1e6, int(mx), int(pk)))
         return out
 
+    def set_timelimit(self, seconds):
+        """Device-clock budget (s) of the following runs; None or 0 removes it."""
+        ns = 0 if not seconds else int(float(seconds) * 1e9)
+        _lib.check(self.L.pdgpu_mc_plan_set_deadline(self._plan, ns), "pdgpu_mc_plan_set_deadline")
+        self.timelimit = seconds
+
     def launch_ms(self):
         """CUDA-event durations (ms) of the last run's transport launches."""
         buf = (C.c_float * 32)()
