@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--packets", type=int, default=1000000, help="packets per model")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-reps", type=int, default=10)
     ap.add_argument("--cpu-models", type=int, default=8)
     ap.add_argument("--cpu-packets", type=int, default=100000)
     ap.add_argument("--timelimit", type=float, default=1800.0,
@@ -137,6 +139,63 @@ def cpu_sample(models, args, threads):
         pk += args.cpu_packets
     dt = time.time() - t0
     return pk / dt, dt
+
+
+def adjoint_rate(dev, seed, reps):
+    """Gradients of an interferometric chi^2 per second (the adjoint workload): disk plus
+    Ulrich envelope on 256 x 256 cells, 1.3 mm image of 256 x 256 pixels spanning +-1.2
+    Rout at 140 pc, inclination uniform in [0, 80] deg, 20,000 uv points (baselines uniform
+    in 10-2000 klambda, uniform position angle), data = model + N(0, 1 mJy).  One gradient
+    = chi^2 and its derivatives w.r.t. every cell density (both species) and (Mdisk, h0,
+    beta, gamma).  Temperatures are frozen (an analytic profile stands in for the thermal
+    run: the cost of a gradient does not depend on the temperature values)."""
+    import torch
+    from pdspy_gb300 import adjoint, vis, workloads
+    rng = np.random.default_rng(seed)
+    m = workloads.disk_envelope(nr=256, ntheta=256)
+    g = m.grid
+    rr = np.meshgrid(g.r, g.theta, g.phi, indexing="ij")[0]
+    g.temperature = [np.maximum(150.0 * rr ** -0.5, 10.0)] * len(g.density)
+    incl = float(rng.uniform(0.0, 80.0))
+    npix, dpc = 256, 140.0
+    pixelsize = 2.4 * 100.0 / dpc / npix        # arcsec: +-1.2 Rout (100 au) across the field
+    u, v = vis.synthetic_uv(20000, seed=seed)
+    nuv = len(u)
+    data = vis.UVData(u, v, np.zeros(nuv), np.zeros(nuv), np.full(nuv, 1.0 / 1e-3 ** 2))
+    prob = adjoint.Chi2Problem(m, data, npix=npix, pixelsize=pixelsize, dpc=dpc, incl=incl,
+                               device=dev)
+    p_true = torch.tensor([1e-2, 0.1, 1.25, 1.0], dtype=torch.float64, device=dev)
+    with torch.no_grad():
+        re, im = prob.visibilities(prob.rho_from_params(p_true, 0.1, 100.0))
+        noise = torch.as_tensor(rng.normal(0.0, 1e-3, (2, nuv)), device=dev)
+        prob.re_d = re.double() + noise[0]
+        prob.im_d = im.double() + noise[1]
+    p = torch.tensor([8e-3, 0.11, 1.2, 0.9], dtype=torch.float64, device=dev)
+
+    def one():
+        pv = p.clone().requires_grad_(True)
+        rho = prob.rho_from_params(pv, 0.1, 100.0)
+        rho.retain_grad()
+        chi = prob.chi2(rho)
+        chi.backward()
+        return chi, pv.grad, rho.grad
+
+    for _ in range(3):
+        one()
+    torch.cuda.synchronize(dev)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        chi, gp, gr = one()
+    b.record()
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    return {"grads_per_s": 1e3 / ms, "ms_per_grad": ms, "unit": "gradients/s",
+            "config": "disk+envelope 256x256 cells, 256x256 px at 1300 um, incl %.1f deg, "
+                      "20000 uv points; d chi2 / d(every cell density, Mdisk, h0, beta, gamma)"
+                      % incl, "chi2": float(chi.item()),
+            "grad_params": [float(x) for x in gp.cpu()]}
 
 
 def workload_name(args):
@@ -276,6 +335,10 @@ def main():
                 "launches_per_step": n_launch, "kernel_ms_per_step": float(np.sum(lm)),
                 "algorithmic_bytes_per_step": int(alg_bytes)}
 
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        adj = adjoint_rate(dev, args.seed, args.adjoint_reps)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_sample(models, args, os.cpu_count())
@@ -300,7 +363,7 @@ def main():
                                      args.warmup_deadline,
                            "geometry": "double-single (FP32 pipe); FP64 energy->temperature",
                            "parallelism": "replicas: independent walker batches per GPU"},
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adj,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
                                             "parked", "drained", "killed", "late_units")},

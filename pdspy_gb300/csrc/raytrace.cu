@@ -6,7 +6,8 @@
 // I = sum_i W_i S_i (1 - exp(-dtau_i)), W_{i+1} = W_i exp(-dtau_i), with per-cell
 // extinction alpha[l][c] and source S[l][c] prepared by the caller, plus point stars at
 // the origin attenuated along the central line of sight.  Ray-wall intersections use the
-// FP64 root solves of mc_geom.cuh; the per-segment radiative transfer is FP32.
+// double-single root solves of mc_geom_ds.cuh (FP32 pipe; the entry point on the outer
+// sphere is computed once per ray in FP64); the per-segment radiative transfer is FP32.
 //
 // Parallel layout: one thread per sub-ray.  Pixels whose rays pass close to cells
 // smaller than the pixel are split into 4^L sub-rays (L from the host, the same rule as
@@ -16,8 +17,8 @@
 // Adjoint: a second sweep along each ray (front to back) recomputes every segment's
 // optical depth and uses the running transmittance W_i and the accumulated intensity
 // Icum_i as checkpoints: dI/dS_i = W_i (1 - e_i), dI/ddtau_i = W_i e_i S_i - (I - Icum_i),
-// where I is the ray's total from the forward pass.  Gradients are accumulated per cell
-// with FP64 atomics.
+// where I is the ray's total from the forward pass.  Per-segment products are FP32; the
+// per-cell sums are FP64 atomics.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,6 +31,7 @@
 #include "mc_common.h"
 #include "mc_device.cuh"
 #include "mc_geom.cuh"
+#include "mc_geom_ds.cuh"
 #include "mc_host.h"
 
 #define RT_MAXL 16
@@ -46,6 +48,7 @@ struct RtCam {
 struct RtParams {
     McModel M;
     const double* dp;
+    const float* fp;      // float wall tables (double-single geometry)
     const float* alpha;   // [nlam_total][ncell]
     const float* S;
     int lam0, nl;         // wavelength chunk [lam0, lam0 + nl)
@@ -70,47 +73,57 @@ __device__ __forceinline__ void sub_uv(const RtCam& C, int px, int py, int sub, 
     v = -X * C.spa + Y * C.cpa;
 }
 
-__device__ bool ray_start(const McModel& M, const double* dp, const RtCam& C, double u, double v,
-                          Pkt& p) {
+__device__ __forceinline__ ds ds_of(double v) {
+    float h = (float)v;
+    return ds{h, (float)(v - (double)h)};
+}
+
+// Entry of a ray into the grid through its outer sphere (FP64, once per ray).
+__device__ bool ray_start(const McModel& M, const double* dp, const float* fp, const RtCam& C,
+                          double u, double v, PktS& p) {
     const double* R = dp + M.off_r;
     double Rm = R[M.nr];
     double D = 1.01 * Rm;
-    p.x = u * C.ex[0] + v * C.ey[0] + D * C.o[0];
-    p.y = u * C.ex[1] + v * C.ey[1] + D * C.o[1];
-    p.z = u * C.ex[2] + v * C.ey[2] + D * C.o[2];
+    double x = u * C.ex[0] + v * C.ey[0] + D * C.o[0];
+    double y = u * C.ex[1] + v * C.ey[1] + D * C.o[1];
+    double z = u * C.ex[2] + v * C.ey[2] + D * C.o[2];
     p.kx = (float)(-C.o[0]);
     p.ky = (float)(-C.o[1]);
     p.kz = (float)(-C.o[2]);
     p.dsafe = 0.0f;
     double kx = (double)p.kx, ky = (double)p.ky, kz = (double)p.kz;
     double kk = kx * kx + ky * ky + kz * kz;
-    double b = p.x * kx + p.y * ky + p.z * kz;
-    double r2 = p.x * p.x + p.y * p.y + p.z * p.z;
+    double b = x * kx + y * ky + z * kz;
+    double r2 = x * x + y * y + z * z;
     double c = r2 - Rm * Rm;
     double D2 = b * b - kk * c;
     if (!(D2 > 0.0) || b >= 0.0) return false;
     double s = c / (sqrt(D2) - b);
-    p.x = fma(s, kx, p.x);
-    p.y = fma(s, ky, p.y);
-    p.z = fma(s, kz, p.z);
+    p.x = ds_of(fma(s, kx, x));
+    p.y = ds_of(fma(s, ky, y));
+    p.z = ds_of(fma(s, kz, z));
     p.ir = M.nr - 1;
-    locate_angles(M, dp, p);
+    WallsS W(M, fp);
+    locate_angles_ds(M, W, p);
     p.last_wall = W_ROUT;
     return true;
 }
 
 // Advance to the next wall; returns false when the ray has left the grid.
-__device__ __forceinline__ bool ray_step(const McModel& M, const double* dp, Pkt& p, int& cell,
-                                         double& len) {
+__device__ __forceinline__ bool ray_step(const McModel& M, const float* fp, PktS& p, int& cell,
+                                         float& len) {
     int wall;
-    len = next_wall(M, dp, p, wall);
-    cell = (p.ir >= 0) ? cell_of(M, p) : -1;
-    p.x = fma(len, (double)p.kx, p.x);
-    p.y = fma(len, (double)p.ky, p.y);
-    p.z = fma(len, (double)p.kz, p.z);
+    WallsS W(M, fp);
+    const ds s = next_wall_ds(M, W, p, wall);
+    len = s.h;
+    cell = (p.ir >= 0 && wall != W_NONE) ? cell_of_s(M, p) : -1;
+    if (wall == W_NONE) return false;   // degenerate ray: no exit found, the ray ends
+    p.x = ds_move2(p.x, s, p.kx);
+    p.y = ds_move2(p.y, s, p.ky);
+    p.z = ds_move2(p.z, s, p.kz);
     switch (wall) {
         case W_ROUT:
-            if (p.ir < 0) { p.ir = 0; locate_angles(M, dp, p); }
+            if (p.ir < 0) { p.ir = 0; locate_angles_ds(M, W, p); }
             else p.ir += 1;
             p.last_wall = W_RIN;
             if (p.ir >= M.nr) return false;
@@ -146,14 +159,14 @@ __global__ void __launch_bounds__(128) rt_forward_kernel(RtParams P) {
         float I[RT_MAXL], W[RT_MAXL];
 #pragma unroll
         for (int l = 0; l < RT_MAXL; ++l) { I[l] = 0.0f; W[l] = 1.0f; }
-        Pkt p;
-        if (ray_start(P.M, P.dp, P.cam, u, v, p)) {
+        PktS p;
+        if (ray_start(P.M, P.dp, P.fp, P.cam, u, v, p)) {
             int cell;
-            double len;
+            float len;
             for (int guard = 0; guard < 100000000; ++guard) {
-                bool more = ray_step(P.M, P.dp, p, cell, len);
+                bool more = ray_step(P.M, P.fp, p, cell, len);
                 if (cell >= 0) {
-                    float lf = (float)len;
+                    float lf = len;
 #pragma unroll
                     for (int l = 0; l < RT_MAXL; ++l) {
                         if (l < P.nl) {
@@ -198,15 +211,15 @@ __global__ void rt_star_kernel(RtParams P, const double* star_flux, double omega
 #pragma unroll
     for (int l = 0; l < RT_MAXL; ++l) tau[l] = 0.0f;
     for (int pass = 0; pass < (adjoint ? 2 : 1); ++pass) {
-        Pkt p;
+        PktS p;
         memset(&p, 0, sizeof(p));
         p.kx = (float)C.o[0]; p.ky = (float)C.o[1]; p.kz = (float)C.o[2];
         p.ir = -1;
         p.last_wall = W_NONE;
         int cell;
-        double len;
+        float len;
         for (int guard = 0; guard < 100000000; ++guard) {
-            bool more = ray_step(P.M, P.dp, p, cell, len);
+            bool more = ray_step(P.M, P.fp, p, cell, len);
             if (cell >= 0) {
                 for (int l = 0; l < P.nl; ++l) {
                     size_t k = (size_t)(P.lam0 + l) * P.ncell + cell;
@@ -215,7 +228,7 @@ __global__ void rt_star_kernel(RtParams P, const double* star_flux, double omega
                     } else {
                         double f = star_flux[P.lam0 + l] * exp(-(double)tau[l]) / omega;
                         double g = P.g_img[(size_t)(P.lam0 + l) * npix + cpix];
-                        atomicAdd(P.g_alpha + k, -g * f * len);
+                        atomicAdd(P.g_alpha + k, -g * f * (double)len);
                     }
                 }
             }
@@ -246,14 +259,17 @@ __global__ void __launch_bounds__(128) rt_adjoint_kernel(RtParams P) {
             It[l] = (l < P.nl) ? P.ray_I[g * RT_MAXL + l] : 0.0f;
             gp[l] = (l < P.nl) ? P.g_img[(size_t)(P.lam0 + l) * npix + pix] * inv : 0.0;
         }
-        Pkt p;
-        if (!ray_start(P.M, P.dp, P.cam, u, v, p)) continue;
+        PktS p;
+        if (!ray_start(P.M, P.dp, P.fp, P.cam, u, v, p)) continue;
         int cell;
-        double len;
+        float len;
+        float gpf[RT_MAXL];
+#pragma unroll
+        for (int l = 0; l < RT_MAXL; ++l) gpf[l] = (float)gp[l];
         for (int guard = 0; guard < 100000000; ++guard) {
-            bool more = ray_step(P.M, P.dp, p, cell, len);
+            bool more = ray_step(P.M, P.fp, p, cell, len);
             if (cell >= 0) {
-                float lf = (float)len;
+                float lf = len;
 #pragma unroll
                 for (int l = 0; l < RT_MAXL; ++l) {
                     if (l < P.nl) {
@@ -268,8 +284,8 @@ __global__ void __launch_bounds__(128) rt_adjoint_kernel(RtParams P) {
                         float dI_ddt = W[l] * e * s - (It[l] - Ic[l]);
                         float dI_dS = W[l] * ome;
                         if (gp[l] != 0.0) {
-                            atomicAdd(P.g_S + k, gp[l] * (double)dI_dS);
-                            atomicAdd(P.g_alpha + k, gp[l] * (double)len * (double)dI_ddt);
+                            atomicAdd(P.g_S + k, (double)(gpf[l] * dI_dS));
+                            atomicAdd(P.g_alpha + k, (double)(gpf[l] * (lf * dI_ddt)));
                         }
                         W[l] = W[l] * e;
                     }
@@ -294,7 +310,7 @@ struct pdgpu_image_plan {
     int64_t nrays;
     double omega;
     int nostar;
-    size_t ws_dp, ws_level, ws_off, ws_star, ws_rayI, ws_total;
+    size_t ws_dp, ws_fp, ws_level, ws_off, ws_star, ws_rayI, ws_total;
     void* uploaded_ws;
     int nsm;
 };
@@ -384,6 +400,7 @@ pdgpu_status pdgpu_image_plan_create(int32_t nr, int32_t ntheta, int32_t nphi,
         return at;
     };
     P->ws_dp = place(P->dp.size() * sizeof(double));
+    P->ws_fp = place(P->fp.size() * sizeof(float));
     P->ws_level = place(P->level.size() * sizeof(int));
     P->ws_off = place(P->off.size() * sizeof(int64_t));
     P->ws_star = place(P->star_flux.size() * sizeof(double));
@@ -415,6 +432,8 @@ pdgpu_status pdgpu_image_plan_upload(pdgpu_image_plan* P, void* ws, size_t bytes
     char* w = (char*)ws;
     if (cudaMemcpyAsync(w + P->ws_dp, P->dp.data(), P->dp.size() * sizeof(double),
                         cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(w + P->ws_fp, P->fp.data(), P->fp.size() * sizeof(float),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(w + P->ws_level, P->level.data(), P->level.size() * sizeof(int),
                         cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(w + P->ws_off, P->off.data(), P->off.size() * sizeof(int64_t),
@@ -432,6 +451,7 @@ static RtParams rt_params(pdgpu_image_plan* P, char* w, const float* alpha, cons
     memset(&r, 0, sizeof(r));
     r.M = P->M;
     r.dp = (const double*)(w + P->ws_dp);
+    r.fp = (const float*)(w + P->ws_fp);
     r.alpha = alpha;
     r.S = S;
     r.ncell = P->M.ncell;
