@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define PDGPU_ABI_VERSION 2
+#define PDGPU_ABI_VERSION 3
 
 typedef int32_t pdgpu_status;
 enum {
@@ -114,9 +114,6 @@ typedef struct {
     int32_t fp64_walls;             /* 0: double-single positions and wall roots (FP32  */
                                     /* pipe, default); 1: the same kernels with FP64    */
                                     /* geometry, the precision reference                */
-    int32_t no_batch;               /* 1: continue long packets one interaction at a    */
-                                    /* time instead of in speculative warp batches      */
-                                    /* (identical results; for timing comparisons)      */
     int64_t drain_below;            /* resumed packets run one per thread until fewer   */
                                     /* than this many are left, then one per warp       */
                                     /* (0 = the warp launch's width, -1 = never)        */

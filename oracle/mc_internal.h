@@ -37,6 +37,7 @@ typedef struct {
     int64_t ncross;
     float dsafe;       /* lower bound of the distance to every wall of the cell */
     float dmax;        /* upper bound of the distance to the nearest wall (ORC_DMAX_UNKNOWN) */
+    int fresh;         /* dsafe was computed at the current position */
     uint32_t ctr[4];   /* [draw block, packet id, model, pass tag] */
     uint32_t key[2];
     uint32_t buf[4];

@@ -772,6 +772,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         p.ir = -1; p.itv = 0; p.ip = 0;
         p.last_wall = W_NONE;
         p.dmax = ORC_DMAX_UNKNOWN;
+        p.fresh = 1;
     }
     for (;;) {
         int c = -1;
@@ -788,6 +789,13 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
         float sef = 0.0f;
         if (alpha > 0.0f) {
             sef = p.tau / alpha;
+            /* a safety distance not computed here is refreshed before a wall solve */
+            if (!(sef < p.dsafe) && !p.fresh) {
+                float D = f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p);
+                p.dsafe = 0.999999f * D;
+                p.dmax = dmax_of(D);
+                p.fresh = 1;
+            }
             if (sef < p.dsafe) { full = 0; se = (double)sef; }
         }
         int wall = W_NONE;
@@ -823,6 +831,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 orc__move_ds(&p, sed, p.kx, p.ky, p.kz);
             }
             p.dsafe = full ? 0.0f : p.dsafe - sef;
+            p.fresh = 0;
             p.last_wall = W_NONE;
             const uint32_t n = (uint32_t)p.nevents;   /* index of this interaction */
             p.cell_events += 1;
@@ -971,11 +980,12 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 }
                 p.tau = -orc_logf(ev[1]);
             }
-            if (did_mrw || (full && !tried))
+            if (did_mrw)
                 Dw = f64 ? wall_distance(G, &p) : orc__wall_distance_ds(G, &p);
-            if (did_mrw || tried || full) {
+            if (did_mrw || tried) {
                 p.dsafe = 0.999999f * Dw;
                 p.dmax = dmax_of(Dw);
+                p.fresh = 1;
             }
             if (p.nevents >= o->max_interactions) { cnt->killed += 1; return p.nevents; }
             if (X->pilot && X->late_after > 0 && p.nevents >= X->late_after) return p.nevents;
@@ -989,8 +999,9 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                 orc__move_ds(&p, swd, p.kx, p.ky, p.kz);
             }
             p.tau = p.tau - tcell;
-            p.dsafe = 0.0f;
+            p.dsafe = 0.0f;          /* on a wall: a wall solve is due */
             p.dmax = ORC_DMAX_UNKNOWN;
+            p.fresh = 1;
             p.ncross += 1;
             cnt->crossings += 1;
             if (X->ccross && c >= 0) atomic_add64(&X->ccross[c], 1);

@@ -33,7 +33,7 @@ class McOptions(C.Structure):
                 ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("late_after", C.c_int64), ("time_launches", C.c_int32),
                 ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int32),
-                ("no_batch", C.c_int32), ("drain_below", C.c_int64)]
+                ("drain_below", C.c_int64)]
 
 
 class McStats(C.Structure):

@@ -21,6 +21,7 @@ struct Pkt {
     double x, y, z;
     float dsafe;    // lower bound of the distance to every wall of the cell
     float dmax;     // upper bound of the distance to the nearest wall (3e38: unknown)
+    int fresh;      // dsafe was computed at the current position
     float kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events;

@@ -95,7 +95,7 @@ struct McParams {
     int64_t drain_below;         // phase 1: drain when fewer are in flight (0 = never)
     int32_t pilot;               // pilot pass: packets stop after late_after events
     int32_t phase;               // 0: epoch launch; 1: parked packets, one per thread;
-                                 // 2: drained packets, one per warp (speculative batches)
+                                 // 2: drained packets, one per warp
     int32_t lslot;               // per-launch debug slot
     int64_t* escape;             // [nm][nl] or null
     int64_t* stats;              // [MC_NSTAT]
@@ -112,7 +112,6 @@ struct McParams {
     int32_t dust_floats, use_smem;
     int32_t o_kabs, o_ksca, o_kext, o_g, o_F, o_cdf, o_kP, o_kR, o_mrw;
     int32_t count_stats;
-    int32_t batch;               // continuation: speculative in-cell batches on/off
 };
 
 struct Cnt {
@@ -479,6 +478,7 @@ __device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, cons
     G::origin(p);
     p.dsafe = 0.0f;
     p.dmax = MC_DMAX_UNKNOWN;
+    p.fresh = 1;
     p.ir = -1; p.itv = 0; p.ip = 0;
     p.last_wall = W_NONE;
     p.cell_events = 0;
@@ -496,7 +496,7 @@ __device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p) 
     r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
     r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag;
     r.spare = __float_as_uint(p.dmax);
-    r.pad[0] = 0; r.pad[1] = 0; r.pad[2] = 0;
+    r.pad[0] = p.fresh; r.pad[1] = 0; r.pad[2] = 0;
 }
 
 template <class G>
@@ -509,6 +509,7 @@ __device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r) 
     p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
     p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag;
     p.dmax = __uint_as_float(r.spare);
+    p.fresh = r.pad[0];
 }
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
@@ -539,6 +540,13 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     float sef = 0.0f;
     if (alpha > 0.0f) {
         sef = p.tau / alpha;
+        // a safety distance not computed here is refreshed before paying for a wall solve
+        if (!(sef < p.dsafe) && !p.fresh) {
+            const float D = pol.template dist<G>(M, dp, P.fpool, p);
+            p.dsafe = 0.999999f * D;
+            p.dmax = mc_dmax_of(D);
+            p.fresh = 1;
+        }
         if (sef < p.dsafe) { full = false; se = G::of(sef); }
     }
     int wall = W_NONE;
@@ -557,6 +565,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     if (is_event) {
         G::move(p, se, p.kx, p.ky, p.kz);
         p.dsafe = full ? 0.0f : p.dsafe - sef;
+        p.fresh = 0;
         p.last_wall = W_NONE;
         const uint32_t n = (uint32_t)p.nevents;   // index of this interaction
         p.cell_events += 1;
@@ -717,10 +726,11 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
             }
             p.tau = ev.tn;
         }
-        if (did_mrw || (full && !tried)) Dw = pol.template dist<G>(M, dp, P.fpool, p);
-        if (did_mrw || tried || full) {
+        if (did_mrw) Dw = pol.template dist<G>(M, dp, P.fpool, p);
+        if (did_mrw || tried) {
             p.dsafe = 0.999999f * Dw;
             p.dmax = mc_dmax_of(Dw);
+            p.fresh = 1;
         }
         if (late) cnt.late += 1;
         if (p.nevents >= P.max_inter) {
@@ -742,8 +752,9 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     }
     G::move(p, sw, p.kx, p.ky, p.kz);
     p.tau = p.tau - tcell;
-    p.dsafe = 0.0f;
+    p.dsafe = 0.0f;          // on a wall: a wall solve is due, nothing to refresh
     p.dmax = MC_DMAX_UNKNOWN;
+    p.fresh = 1;
     p.ncross += 1;
     cnt.crossings += 1;
     p.cell_events = 0;
@@ -770,307 +781,6 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         return false;
     }
     return true;
-}
-
-// Shuffle of a register-resident struct, word by word.
-template <class S>
-__device__ __forceinline__ S shfl_struct(const S& v, int src) {
-    static_assert(sizeof(S) % 4 == 0, "word-sized struct");
-    S out;
-    const uint32_t* a = reinterpret_cast<const uint32_t*>(&v);
-    uint32_t* b = reinterpret_cast<uint32_t*>(&out);
-#pragma unroll
-    for (int i = 0; i < (int)(sizeof(S) / 4); ++i) b[i] = __shfl_sync(0xffffffffu, a[i], src);
-    return out;
-}
-
-// Speculative batch of in-cell interactions of one packet owned by a whole warp.
-//
-// Because every interaction draws from its own Philox blocks, lane j can prepare
-// interaction n0 + j before the ones in front of it are known: its random numbers, the new
-// optical depth, the isotropic direction and the reemission wavelength an absorption would
-// give (the cell, and so its temperature snapshot, is fixed inside a batch).  One cheap
-// sequential pass then chains wavelength, direction and position through the batch
-// assuming every interaction stays in the cell; the expensive checks run on all lanes at
-// once: the wall distance after each interaction (MRW test and safety-distance refresh)
-// and, for interactions that the safety distance cannot clear, the full wall solve.  The
-// first MRW jump ends the batch and is carried out by its lane with the values already at
-// hand.  The batch is cut before the first interaction that leaves the cell or is placed
-// on a wall; the caller runs that one through the general step.  The committed
-// interactions are identical, operation for operation, to running the general step one by
-// one.
-//
-// Returns the number of interactions committed and sets *cut when the batch stopped
-// before an interaction that needs the general step; returns -1 when the packet's state
-// does not allow a batch.
-template <int NS, class G>
-__device__ int seb_batch(typename G::Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt,
-                         int lane, int bmax, bool* cut) {
-    using Pk = typename G::Pkt;
-    using len_t = typename G::len_t;
-    const unsigned FULL = 0xffffffffu;
-    *cut = true;
-    if (p.ir < 0) return -1;
-    const McModel& M = P.models[p.m];
-    const double* __restrict__ dp = P.dpool;
-    const int nl = P.nl;
-    const uint32_t k0 = P.key0, k1 = P.key1;
-    int B = bmax < 32 ? bmax : 32;
-    const long long room = (long long)P.max_inter - 1 - (long long)p.nevents;
-    if (room < (long long)B) B = room > 0 ? (int)room : 0;
-    if (B <= 0) return -1;
-    const int c = G::cell(M, p);
-    const int64_t base = M.cell_off;
-    float rh[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) rh[s] = __ldg(P.rho + base + (int64_t)s * M.ncell + c);
-    const float2* qa = P.q + (int64_t)p.epoch * P.qstride;
-    float2 qv[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) qv[s] = qa[base + (int64_t)s * M.ncell + c];
-    LanePol lp;
-    float aR = 0.0f;
-    if (P.mrw) {
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-            aR = aR + rh[s] * row_interp(lp, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
-    }
-    // phase 1: lane j prepares interaction n0 + j
-    const uint32_t n0 = (uint32_t)p.nevents;
-    float ua = 0.0f, tn = 0.0f, umu = 0.0f, cs = 1.0f, sn = 0.0f, kix = 0.0f, kiy = 0.0f,
-          kiz = 1.0f, us = 0.0f;
-    int la[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) la[s] = 0;
-    if (lane < B) {
-        const uint4 ev = mc_block(p.rng, n0 + (uint32_t)lane, MC_RS_EVENT, k0, k1);
-        const uint4 sb = mc_block(p.rng, n0 + (uint32_t)lane, MC_RS_SECOND, k0, k1);
-        ua = mc_u01(ev.x);
-        tn = -mc_logf(mc_u01(ev.y));
-        umu = mc_u01(ev.z);
-        mc_sincospif2(mc_u01(ev.w), sn, cs);
-        float mu = 2.0f * umu - 1.0f;
-        float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
-        kix = st * cs; kiy = st * sn; kiz = mu;
-        us = mc_u01(sb.w);
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-            la[s] = reemit_lambda(lp, T, nl, qv[s], s, mc_u01(sb.x), mc_u01(sb.y), mc_u01(sb.z));
-    }
-    // phase 2: sequential chain, identical in every lane; lane j keeps interaction j
-    Pk q = p;
-    Pk pre = p, post = p;
-    float my_alpha = 0.0f, my_sef = 0.0f;
-    int my_abs = 0, my_sp = 0;
-    for (int j = 0; j < B; ++j) {
-        float a = 0.0f;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) a = a + rh[s] * T.kext[s * nl + q.lam];
-        if (!(a > 0.0f)) { B = j; break; }
-        const float sef = q.tau / a;
-        if (lane == j) { pre = q; my_alpha = a; my_sef = sef; }
-        G::move(q, G::of(sef), q.kx, q.ky, q.kz);
-        q.last_wall = W_NONE;
-        q.cell_events += 1;
-        q.nevents += 1;
-        const float ua_j = __shfl_sync(FULL, ua, j);
-        const float us_j = (NS > 1) ? __shfl_sync(FULL, us, j) : 0.0f;
-        float asca = 0.0f;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) asca = asca + rh[s] * T.ksca[s * nl + q.lam];
-        if (ua_j * a < asca) {
-            int sp = 0;
-            if (NS > 1) {
-                float usv = us_j * asca;
-                float acc = 0.0f;
-                sp = NS - 1;
-#pragma unroll
-                for (int s = 0; s < NS; ++s) {
-                    acc = acc + rh[s] * T.ksca[s * nl + q.lam];
-                    if (usv < acc) { sp = s; break; }
-                }
-            }
-            const float g = T.g[sp * nl + q.lam];
-            const float umu_j = __shfl_sync(FULL, umu, j);
-            const float cs_j = __shfl_sync(FULL, cs, j);
-            const float sn_j = __shfl_sync(FULL, sn, j);
-            float mu;
-            if (fabsf(g) < 1.0e-4f) {
-                mu = 2.0f * umu_j - 1.0f;
-            } else {
-                float t = (1.0f - g * g) / (1.0f - g + 2.0f * g * umu_j);
-                mu = (1.0f + g * g - t * t) / (2.0f * g);
-                if (mu < -1.0f) mu = -1.0f;
-                if (mu > 1.0f) mu = 1.0f;
-            }
-            mc_rotate(q.kx, q.ky, q.kz, mu, cs_j, sn_j);
-            if (lane == j) my_abs = 0;
-        } else {
-            int sp = 0;
-            if (NS > 1) {
-                float aabs = 0.0f;
-#pragma unroll
-                for (int s = 0; s < NS; ++s) aabs = aabs + rh[s] * T.kabs[s * nl + q.lam];
-                float usv = us_j * aabs;
-                float acc = 0.0f;
-                sp = NS - 1;
-#pragma unroll
-                for (int s = 0; s < NS; ++s) {
-                    acc = acc + rh[s] * T.kabs[s * nl + q.lam];
-                    if (usv < acc) { sp = s; break; }
-                }
-            }
-            int lsel = la[0];
-#pragma unroll
-            for (int s = 1; s < NS; ++s)
-                if (s == sp) lsel = la[s];
-            q.lam = __shfl_sync(FULL, lsel, j);
-            q.kx = __shfl_sync(FULL, kix, j);
-            q.ky = __shfl_sync(FULL, kiy, j);
-            q.kz = __shfl_sync(FULL, kiz, j);
-            if (lane == j) { my_abs = 1; my_sp = sp; }
-        }
-        q.tau = __shfl_sync(FULL, tn, j);
-        if (lane == j) post = q;
-    }
-    if (B <= 0) return -1;
-    // phase 3: wall distance after each interaction
-    float D = 0.0f;
-    if (lane < B) D = G::dist(M, dp, P.fpool, post);
-    // phase 4: replay of the safety distance, the distance bound and the MRW decisions
-    float dsf = p.dsafe, dmx = p.dmax;
-    int Jm = B;   // first MRW jump
-    bool my_full = false;
-    float my_dsafe = 0.0f, my_dmax = 0.0f;
-    for (int j = 0; j < B; ++j) {
-        const float sef_j = __shfl_sync(FULL, my_sef, j);
-        const float D_j = __shfl_sync(FULL, D, j);
-        const float a_j = __shfl_sync(FULL, my_alpha, j);
-        const int ce_j = p.cell_events + j + 1;
-        const int nv_j = p.nevents + j + 1;
-        const bool full = !(sef_j < dsf);
-        dmx = mc_dmax_after(dmx, sef_j);
-        const bool cond = P.mrw && (ce_j >= P.mrw_trigger ||
-                                    (P.mrw_eager_after > 0 && nv_j > P.mrw_eager_after));
-        bool tried = false;
-        if (cond && 0.999f * dmx * a_j >= P.mrw_tauthres) tried = 0.999f * dmx * aR >= P.mrw_gamma;
-        const float R0f = 0.999f * D_j;
-        if (lane == j) my_full = full;
-        if (tried && R0f * aR >= P.mrw_gamma && R0f * a_j >= P.mrw_tauthres) { Jm = j; break; }
-        if (full || tried) {
-            dsf = 0.999999f * D_j;
-            dmx = mc_dmax_of(D_j);
-        } else {
-            dsf = dsf - sef_j;
-        }
-        if (lane == j) { my_dsafe = dsf; my_dmax = dmx; }
-    }
-    const unsigned live = (B >= 32) ? FULL : ((1u << B) - 1u);
-    const int Jr = Jm < B ? Jm + 1 : B;
-    // phase 5: wall solves of the interactions the safety distance did not clear
-    bool bad = false;
-    if (lane < Jr && my_full) {
-        int w;
-        const len_t sw = G::wall_lane(M, dp, P.fpool, pre, w);
-        const float tcell = my_alpha * G::f(sw);
-        bad = !(tcell > pre.tau) || G::gt(G::of(my_sef), sw);
-    }
-    const unsigned badm = __ballot_sync(FULL, bad) & live;
-    const int Jb = badm ? (__ffs(badm) - 1) : B;
-    const bool jump = Jm < B && Jb > Jm;    // the batch ends with an MRW jump
-    const int J = jump ? Jm : min(Jm, Jb);
-    *cut = !jump && J < B;
-    // commit interactions 0..J-1
-    const bool mine = lane < J;
-    const bool late = P.late_after > 0 && post.nevents > P.late_after;
-    if (mine && my_abs) {
-        int64_t* dep = late ? P.Elate : P.E;
-        atomicAdd((unsigned long long*)(dep + base + (int64_t)my_sp * M.ncell + c),
-                  1ull << MC_EUNIT_SHIFT);
-    }
-    const int nabs = __popc(__ballot_sync(FULL, mine && my_abs));
-    const int nlate = __popc(__ballot_sync(FULL, mine && late));
-    cnt.events += J;
-    cnt.absorb += nabs;
-    cnt.scatter += J - nabs;
-    cnt.late += nlate;
-    if (!jump) {
-        if (J > 0) {
-            p = shfl_struct(post, J - 1);
-            p.dsafe = __shfl_sync(FULL, my_dsafe, J - 1);
-            p.dmax = __shfl_sync(FULL, my_dmax, J - 1);
-        }
-        return J;
-    }
-    // the MRW jump of interaction Jm, computed by its lane (as in the general step)
-    Pk m = post;
-    if (lane == Jm) {
-        const uint4 mb = mc_block(p.rng, n0 + (uint32_t)Jm, MC_RS_MRW, k0, k1);
-        const float R0f = 0.999f * D;
-        const len_t R0 = G::of(R0f);
-        float uy = mc_u01(mb.x);
-        float f = uy * (float)(MC_NMRW - 1);
-        int i = (int)f;
-        if (i > MC_NMRW - 2) i = MC_NMRW - 2;
-        float w = f - (float)i;
-        float yv = T.mrw[i] + w * (T.mrw[i + 1] - T.mrw[i]);
-        float ell = 3.0f * aR * R0f * R0f * yv;
-        int64_t* dep = late ? P.Elate : P.E;
-        float kp[NS];
-        float aP = 0.0f;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            kp[s] = rh[s] * row_interp(lp, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
-            aP = aP + kp[s];
-            float units_f = kp[s] * ell * 1048576.0f + 0.5f;
-            if (units_f > 9.0e18f) units_f = 9.0e18f;
-            long long units = (long long)units_f;
-            if (units > 0)
-                atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
-                          (unsigned long long)units);
-        }
-        float dx, dy, dz;
-        {
-            float mu = 2.0f * mc_u01(mb.y) - 1.0f;
-            float sn2, cs2;
-            mc_sincospif2(mc_u01(mb.z), sn2, cs2);
-            float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
-            dx = st * cs2; dy = st * sn2; dz = mu;
-        }
-        G::move(m, R0, dx, dy, dz);
-        {
-            float mu = sqrtf(umu);
-            float kx = dx, ky = dy, kz = dz;
-            mc_rotate(kx, ky, kz, mu, cs, sn);
-            m.kx = kx; m.ky = ky; m.kz = kz;
-        }
-        int sp = 0;
-        if (NS > 1) {
-            float usv = us * aP;
-            float acc = 0.0f;
-            sp = NS - 1;
-#pragma unroll
-            for (int s = 0; s < NS; ++s) {
-                acc = acc + kp[s];
-                if (usv < acc) { sp = s; break; }
-            }
-        }
-        int lsel = la[0];
-#pragma unroll
-        for (int s = 1; s < NS; ++s)
-            if (s == sp) lsel = la[s];
-        m.lam = lsel;
-        m.tau = tn;
-        m.cell_events = 0;
-        const float D2 = G::dist(M, dp, P.fpool, m);
-        m.dsafe = 0.999999f * D2;
-        m.dmax = mc_dmax_of(D2);
-    }
-    p = shfl_struct(m, Jm);
-    cnt.events += 1;
-    cnt.mrw += 1;
-    if (__shfl_sync(FULL, late, Jm)) cnt.late += 1;
-    return J + 1;
 }
 
 __device__ __forceinline__ long long warp_sum(long long v) {
@@ -1280,17 +990,8 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         park_load<G>(p, P.park_in[g]);
         WarpPol pol(lane);
         bool alive = true;
-        // batch length follows the recent run length between interruptions (a batch planned
-        // much longer only adds sequential work that is thrown away)
-        float run = 8.0f;
         while (alive) {
-            bool cut = true;
-            if (P.batch) {
-                const int bmax = min(32, max(4, (int)(2.0f * run) + 2));
-                const int got = seb_batch<NS, G>(p, P, T, cnt, lane, bmax, &cut);
-                if (got >= 0) run = 0.75f * run + 0.25f * (float)got;
-            }
-            if (cut) alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
+            alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
                 if (lane == 0) {
@@ -1903,7 +1604,6 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.o_F = P->o_F; prm.o_cdf = P->o_cdf; prm.o_kP = P->o_kP; prm.o_kR = P->o_kR;
     prm.o_mrw = P->o_mrw;
     prm.count_stats = final_pass ? 1 : 0;
-    prm.batch = P->opt.no_batch ? 0 : 1;
     if (prm.total <= 0) return PDGPU_OK;
     void (*kern)(McParams) = nullptr;
     const bool f64 = P->opt.fp64_walls != 0;

@@ -140,7 +140,7 @@ class ThermalPlan:
                  max_interactions=DEFAULTS["max_interactions"], late_after=DEFAULTS["late_after"],
                  mrw_eager_after=DEFAULTS["mrw_eager_after"], timelimit=None, device=None,
                  block_threads=0, blocks_per_sm=0, abort_flag=None, time_launches=False,
-                 fp64_walls=False, no_batch=False, drain_below=0):
+                 fp64_walls=False, drain_below=0):
         if not isinstance(grids, (list, tuple)):
             grids = [grids]
         self.L = _lib.lib()
@@ -183,7 +183,7 @@ class ThermalPlan:
                                    abort_flag, int(block_threads), int(blocks_per_sm),
                                    int(late_after), int(bool(time_launches)),
                                    int(mrw_eager_after), int(bool(fp64_walls)),
-                                   int(bool(no_batch)), int(drain_below))
+                                   int(drain_below))
         self.timelimit = timelimit
         self._plan = C.c_void_p()
         with torch.cuda.device(self.device):
@@ -328,7 +328,7 @@ def _options(keywords):
         opts["mrw"] = bool(kw.pop("modified_random_walk"))
     for k in ("mrw_gamma", "mrw_tauthres", "mrw_count_trigger", "nepoch", "npilot",
               "max_interactions", "block_threads", "blocks_per_sm", "late_after",
-              "mrw_eager_after", "fp64_walls", "no_batch", "drain_below"):
+              "mrw_eager_after", "fp64_walls", "drain_below"):
         if k in kw:
             opts[k] = kw.pop(k)
     if "timelimit" in kw:
@@ -372,3 +372,64 @@ def run_thermal_batched(models, nphot=1e6, **keywords):
     for m, temps in zip(models, plan.split(Th)):
         m.grid.temperature = temps
     return stats
+
+
+# Schedule knobs of a thermal plan.  Every setting gives identical results (the walk does
+# not depend on which thread or warp runs it); only the time changes.
+SCHEDULES = [
+    dict(),
+    dict(block_threads=128),
+    dict(blocks_per_sm=1),
+    dict(drain_below=-1),
+    dict(drain_below=16384),
+    dict(drain_below=4096),
+]
+
+
+def autotune(models, nphot, probe_nphot=20000, schedules=None, cache=None, **keywords):
+    """Block and queue schedule for a (batched) thermal run, chosen by timing a short run of
+    each candidate schedule on the same models with ``probe_nphot`` packets per model.
+
+    Returns ``(best_schedule, timings_ms)``.  With ``cache`` (a JSON file path) the choice
+    is stored under a key of the device name, the number of models and cells and the packet
+    count, and reused.  The schedule is a dict of ThermalPlan keywords."""
+    import json
+    import os
+    schedules = SCHEDULES if schedules is None else schedules
+    opts = _options(keywords)
+    grids = [m.grid for m in models]
+    ncell = int(sum(np.asarray(g.density[0]).size * len(g.density) for g in grids))
+    key = "%s|%d|%d|%d" % (torch.cuda.get_device_name(), len(grids), ncell, int(nphot))
+    if cache and os.path.exists(cache):
+        try:
+            known = json.load(open(cache))
+            if key in known:
+                return dict(known[key]["schedule"]), known[key]["timings_ms"]
+        except (OSError, ValueError):
+            pass
+    rho_h = np.concatenate([stack_density(g).reshape(-1) for g in grids])
+    timings = []
+    for sched in schedules:
+        plan = ThermalPlan(grids, probe_nphot, **opts, **sched)
+        rho, T = plan.new_buffers()
+        rho.copy_(torch.from_numpy(rho_h))
+        plan.run(rho, T)                      # warm-up (module load, caches)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        plan.run(rho, T)
+        b.record()
+        torch.cuda.synchronize()
+        plan.check_status()
+        timings.append(a.elapsed_time(b))
+    best = dict(schedules[int(np.argmin(timings))])
+    if cache:
+        try:
+            known = json.load(open(cache)) if os.path.exists(cache) else {}
+        except (OSError, ValueError):
+            known = {}
+        known[key] = {"schedule": best, "timings_ms": timings}
+        with open(cache, "w") as f:
+            json.dump(known, f, indent=1)
+    return best, timings

@@ -58,11 +58,11 @@ def test_fp64_geometry_bit_exact(cuda, name):
         assert st[k] == ref["stats"][k], (name, k)
 
 
-@pytest.mark.parametrize("variant", [dict(no_batch=True), dict(drain_below=-1),
-                                     dict(drain_below=10 ** 9)])
+@pytest.mark.parametrize("variant", [dict(drain_below=-1), dict(drain_below=10 ** 9),
+                                     dict(block_threads=128, blocks_per_sm=1)])
 def test_continuation_schedules_change_nothing(cuda, variant):
-    """Resumed long walks: one per thread, drained to one per warp, in speculative warp
-    batches or one interaction at a time -- the same interactions either way."""
+    """Resumed long walks one per thread or drained to one per warp, and other block
+    schedules -- the same interactions either way."""
     models = workloads.walker_models(n=4, seed=8, scale=0.2)
     kw = dict(seed=4, mrw=True, mrw_count_trigger=10, late_after=60, mrw_eager_after=120)
     _, E1, T1, s1 = _gpu_run(models, 3000, **kw)
@@ -114,3 +114,17 @@ def test_graph_replay_reproduces(cuda):
     assert torch.equal(E1, plan.energy())
     ref = _cases.run_oracle(m, 3000, seed=9)
     assert np.array_equal(E1.cpu().numpy(), ref["energy"].reshape(-1))
+
+
+def test_autotune_picks_a_schedule_and_caches_it(cuda, tmp_path):
+    models = workloads.walker_models(n=3, seed=5, scale=0.15)
+    cache = str(tmp_path / "sched.json")
+    best, times = thermal.autotune(models, 3000, probe_nphot=1500, cache=cache,
+                                   modified_random_walk=True, mrw_count_trigger=20)
+    assert best in thermal.SCHEDULES and len(times) == len(thermal.SCHEDULES)
+    again, t2 = thermal.autotune(models, 3000, cache=cache)
+    assert again == best and t2 == times
+    # the chosen schedule gives the same temperatures as the default one
+    _, E1, T1, _ = _gpu_run(models, 3000, seed=1, mrw=True, **best)
+    _, E2, T2, _ = _gpu_run(models, 3000, seed=1, mrw=True)
+    assert np.array_equal(E1, E2) and np.array_equal(T1, T2)
