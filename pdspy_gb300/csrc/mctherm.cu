@@ -1443,7 +1443,9 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->ws_D = place((size_t)P->total_cells * sizeof(int64_t));
     P->ws_q = place((size_t)P->K * P->total_cells * sizeof(float2));
     P->ws_Elate = place((size_t)P->total_cells * sizeof(int64_t));
-    P->park_cap = std::max<int64_t>(8192, P->total_nphot / 128);
+    // room for every packet that outlives late_after in heavy-tailed runs (about 1 in 100
+    // in the densest disks); a packet that finds the list full finishes in its epoch launch
+    P->park_cap = std::max<int64_t>(65536, P->total_nphot / 16);
     P->ws_park = place((size_t)P->park_cap * sizeof(ParkRec));
     P->ws_park2 = place((size_t)P->park_cap * sizeof(ParkRec));
     // [parked after late_after, drained for the warp-per-packet launch, in flight, spare]
