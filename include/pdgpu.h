@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define PDGPU_ABI_VERSION 3
+#define PDGPU_ABI_VERSION 4
 
 typedef int32_t pdgpu_status;
 enum {
@@ -267,6 +267,57 @@ pdgpu_status pdgpu_vis_dft_adjoint(int32_t nx, int32_t ny, double x0_rad, double
                                    double y0_rad, double dy_rad, int32_t nuv, const float* u,
                                    const float* v, const double* grad_re,
                                    const double* grad_im, double* grad_image, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Monte Carlo scattering source (images and spectra at albedo > 0)           */
+/* ------------------------------------------------------------------------- */
+
+/* Controls of the monochromatic scattering Monte Carlo RADMC-3D runs before "radmc3d
+ * image" / "radmc3d spectrum" when the dust scatters, and as "radmc3d mcscat" behind
+ * Model.run_scattering (pdspy/modeling/Model.py:258-322, pdspy/radmc3d/run.py:40-67).
+ * The keywords pdspy writes to radmc3d.inp map to: nphot_scat / nphot_spec
+ * (radmc3d/write.py:33-34; Model.py:520 passes run_image's nphot) -> nphot, and
+ * mc_scat_maxtauabs (write.py:141-142) -> maxtauabs.  Scattering is isotropic: pdspy
+ * writes dustkappa files without the asymmetry parameter (Model.py:774-776). */
+typedef struct pdgpu_scat_options {
+    uint64_t seed;
+    int64_t nphot;            /* packets per wavelength                                  */
+    float maxtauabs;          /* a packet is dropped once the absorption optical depth   */
+                              /* along its path exceeds this (<= 0: 30)                  */
+    int32_t max_scatter;      /* scatterings per packet before it is dropped (<= 0: 1e6) */
+    int32_t block_threads;    /* 0: 256                                                  */
+    int32_t blocks_per_sm;    /* 0: from the occupancy calculator                       */
+} pdgpu_scat_options;
+
+typedef struct pdgpu_scat_stats {
+    int64_t packets, escaped, dropped, capped, scatterings, crossings;
+    int32_t status;
+} pdgpu_scat_stats;
+
+typedef struct pdgpu_scat_plan pdgpu_scat_plan;
+
+/* One grid (model->nr.. phi_edges, the stars of model; model->nphot is ignored), nlam
+ * wavelengths (microns) and the opacities there (host double [nspec][nlam], cm^2/g). */
+pdgpu_status pdgpu_scat_plan_create(const pdgpu_model_desc* model, int32_t nlam,
+                                    const double* lam_um, int32_t nspec, const double* kabs,
+                                    const double* ksca, const pdgpu_scat_options* opts,
+                                    pdgpu_scat_plan** plan);
+void pdgpu_scat_plan_destroy(pdgpu_scat_plan* plan);
+pdgpu_status pdgpu_scat_plan_info(const pdgpu_scat_plan* plan, size_t* workspace_bytes,
+                                  int64_t* ncell);
+pdgpu_status pdgpu_scat_plan_upload(pdgpu_scat_plan* plan, void* workspace, size_t bytes,
+                                    void* stream);
+/* Mean intensity of the radiation field in every cell at every wavelength, J (device
+ * double [nlam][ncell], erg/s/cm^2/Hz/ster), from packets emitted by the stars and, when
+ * emis is given, by the dust (device double [nlam][ncell], thermal emissivity
+ * sum_s rho_s kabs_s B_nu(T), erg/s/cm^3/Hz/ster).  rho: device float [nspec][ncell].
+ * The isotropic scattering source of a cell is sum_s rho_s ksca_s J.  Enqueues kernels
+ * and memsets only. */
+pdgpu_status pdgpu_scat_run(pdgpu_scat_plan* plan, const float* rho, const double* emis,
+                            double* J, void* workspace, size_t bytes, void* stream);
+/* Counters of the last run (synchronises the stream); stats->status as pdgpu_status. */
+pdgpu_status pdgpu_scat_plan_stats(pdgpu_scat_plan* plan, const void* workspace, void* stream,
+                                   pdgpu_scat_stats* stats);
 
 #ifdef __cplusplus
 }

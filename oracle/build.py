@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liborc.so")
-SOURCES = ["mcrt_oracle.c", "geom_ds.c", "raytrace_oracle.c"]
+SOURCES = ["mcrt_oracle.c", "geom_ds.c", "raytrace_oracle.c", "mcscat_oracle.c"]
 CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
           "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 

@@ -1,9 +1,9 @@
 /*
- * CPU oracle for the thermal Monte Carlo and the ray-traced images of pdspy's
- * Model.run_thermal / Model.run_image (radmc3d branch, pdspy/modeling/Model.py:221-256,
- * :515-577).  TEST INFRASTRUCTURE ONLY: only tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py may load this library, and only as the checker or as
- * the timed CPU baseline.  The product (pdspy_gb300) never links or calls it.
+ * CPU oracle for the thermal Monte Carlo, the scattering Monte Carlo and the ray-traced
+ * images of pdspy's Model.run_thermal / run_scattering / run_image (radmc3d branch,
+ * pdspy/modeling/Model.py:221-256, :258-322, :515-577).  TEST INFRASTRUCTURE ONLY: only
+ * tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py may load this
+ * library, and only as the checker or as the timed CPU baseline.  The product (pdspy_gb300) never links or calls it.
  *
  * The arithmetic inside pdspy's radmc3d branch lives in the external RADMC-3D binary,
  * whose source is not part of pdspy and is not pinned by it (pdspy/radmc3d/run.py:9-38
@@ -117,6 +117,37 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
                 const float* rho, const orc_opts* opts, int64_t* energy,
                 double* temperature, int64_t* escape, int64_t* cell_crossings,
                 orc_stats* stats);
+
+/* Scattering Monte Carlo (mcscat_oracle.c): mean intensity J per cell and wavelength. */
+typedef struct {
+    int64_t nphot;                /* packets per wavelength                        */
+    uint64_t seed;
+    float maxtauabs;              /* drop a packet beyond this absorption depth    */
+                                  /* (<= 0: 30)                                    */
+    int max_scatter;              /* scatterings before a packet is dropped (<= 0: */
+                                  /* 1e6)                                          */
+    int nthreads;                 /* OpenMP threads (0 = all)                      */
+} orc_scat_opts;
+
+typedef struct {
+    int64_t packets, escaped, dropped, capped, scatterings, crossings;
+} orc_scat_stats;
+
+/* exp(-x) for x >= 0, (1 - exp(-x)) / x given e = exp(-x), and the cube root on (0, 1]
+ * as the scattering walk evaluates them (exposed for unit tests). */
+float orc_expm(float x);
+float orc_expm_frac(float x, float e);
+float orc_cbrt01(float x);
+
+/* J[nlam][ncell] (erg/s/cm^2/Hz/ster) at wavelengths lam_um (microns) for opacities
+ * kabs/ksca [nspec][nlam] (cm^2/g), densities rho [nspec][ncell] (g/cm^3), the stars
+ * (at the origin) and, when emis is not NULL, the thermal emissivity of the cells
+ * emis[nlam][ncell] (erg/s/cm^3/Hz/ster).  acc_out (optional, int64 [nlam][ncell])
+ * receives the fixed-point path sums.  Returns 0 on success, 1 on invalid input. */
+int orc_mcscat(const orc_grid* grid, int nlam, const double* lam_um, int nspec,
+               const double* kabs, const double* ksca, const orc_stars* stars,
+               const float* rho, const double* emis, const orc_scat_opts* opts, double* J,
+               int64_t* acc_out, orc_scat_stats* stats);
 
 #ifdef __cplusplus
 }

@@ -66,6 +66,13 @@ def lib():
         _lib.orc_build_tables.restype = C.c_double
         _lib.orc_logf.restype = C.c_float
         _lib.orc_logf.argtypes = [C.c_float]
+        _lib.orc_expm.restype = C.c_float
+        _lib.orc_expm.argtypes = [C.c_float]
+        _lib.orc_expm_frac.restype = C.c_float
+        _lib.orc_expm_frac.argtypes = [C.c_float, C.c_float]
+        _lib.orc_cbrt01.restype = C.c_float
+        _lib.orc_cbrt01.argtypes = [C.c_float]
+        _lib.orc_mcscat.restype = C.c_int
     return _lib
 
 
@@ -83,6 +90,18 @@ def philox(ctr, key):
 
 def logf(x):
     return lib().orc_logf(C.c_float(x))
+
+
+def expm(x):
+    return lib().orc_expm(C.c_float(x))
+
+
+def expm_frac(x, e):
+    return lib().orc_expm_frac(C.c_float(x), C.c_float(e))
+
+
+def cbrt01(x):
+    return lib().orc_cbrt01(C.c_float(x))
 
 
 def sincospif2(u):
@@ -166,6 +185,48 @@ def mctherm(r_edges, th_edges, ph_edges, rho, lam_um, kabs, ksca, g, star_radius
     if cc is not None:
         out["crossings"] = cc.reshape(shape[1:])
     return out
+
+
+class ScatOpts(C.Structure):
+    _fields_ = [("nphot", C.c_int64), ("seed", C.c_uint64), ("maxtauabs", C.c_float),
+                ("max_scatter", C.c_int), ("nthreads", C.c_int)]
+
+
+class ScatStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("packets", "escaped", "dropped", "capped",
+                                         "scatterings", "crossings")]
+
+    def asdict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+def mcscat(r_edges, th_edges, ph_edges, rho, lam_um, kabs, ksca, star_radius, star_temp,
+           nphot, emis=None, seed=0, maxtauabs=30.0, max_scatter=0, nthreads=0):
+    """Scattering Monte Carlo oracle: dict(J [nlam, ncell], acc [nlam, ncell] int64,
+    stats).  kabs/ksca [nspec, nlam] at lam_um; rho [nspec, ncell]; emis [nlam, ncell]."""
+    keep = _Keep()
+    g = _grid(r_edges, th_edges, ph_edges, keep)
+    lam = keep.arr(np.atleast_1d(lam_um))
+    ka = keep.arr(np.atleast_2d(kabs)); ks = keep.arr(np.atleast_2d(ksca))
+    ns, nl = ka.shape
+    assert nl == len(lam) and ks.shape == ka.shape
+    sr = keep.arr(np.atleast_1d(star_radius)); stt = keep.arr(np.atleast_1d(star_temp))
+    stars = Stars(len(sr), _dp(sr), _dp(stt))
+    ncell = g.nr * g.nt * g.np
+    r = np.ascontiguousarray(np.asarray(rho, dtype=np.float32).reshape(ns, ncell))
+    e = None
+    if emis is not None:
+        e = keep.arr(np.asarray(emis, dtype=np.float64).reshape(nl, ncell))
+    J = np.zeros((nl, ncell))
+    acc = np.zeros((nl, ncell), np.int64)
+    o = ScatOpts(int(nphot), int(seed), float(maxtauabs), int(max_scatter), int(nthreads))
+    st = ScatStats()
+    rc = lib().orc_mcscat(C.byref(g), nl, _dp(lam), ns, _dp(ka), _dp(ks), C.byref(stars),
+                          r.ctypes.data_as(C.c_void_p), _dp(e) if e is not None else None,
+                          C.byref(o), _dp(J), acc.ctypes.data_as(C.c_void_p), C.byref(st))
+    if rc:
+        raise ValueError("oracle rejected the input (rc=%d)" % rc)
+    return dict(J=J, acc=acc, stats=st.asdict())
 
 
 class Camera(C.Structure):

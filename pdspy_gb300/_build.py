@@ -1,8 +1,8 @@
 """In-tree build of the CUDA library ``pdspy_gb300/_build/libpdgpu.so`` (sm_103a).
 
 Each translation unit is compiled by nvcc in parallel and linked into one shared
-library that exports the C ABI declared in ``include/pdgpu.h``.  The thermal Monte Carlo
-unit is compiled with ``--fmad=false`` and host ``-ffp-contract=off`` so that every
+library that exports the C ABI declared in ``include/pdgpu.h``.  The Monte Carlo and
+ray-tracing units are compiled with ``--fmad=false`` and host ``-ffp-contract=off`` so that every
 floating-point operation is a single IEEE operation (the walk is bit-reproducible and
 comparable operation for operation with the CPU oracle); the other units use the
 default contraction.
@@ -24,6 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("mctherm.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("raytrace.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("mcscat.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("dft.cu", []),
 ]
 HEADERS = ["mc_common.h", "mc_device.cuh", "mc_geom.cuh", "mc_geom_ds.cuh", "mc_host.h"]

@@ -55,6 +55,21 @@ class McLayout(C.Structure):
                 ("smem_tables", C.c_int32)]
 
 
+class ScatOptions(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("nphot", C.c_int64), ("maxtauabs", C.c_float),
+                ("max_scatter", C.c_int32), ("block_threads", C.c_int32),
+                ("blocks_per_sm", C.c_int32)]
+
+
+class ScatStats(C.Structure):
+    _fields_ = [("packets", C.c_int64), ("escaped", C.c_int64), ("dropped", C.c_int64),
+                ("capped", C.c_int64), ("scatterings", C.c_int64), ("crossings", C.c_int64),
+                ("status", C.c_int32)]
+
+    def asdict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
 class Camera(C.Structure):
     _fields_ = [("npix_x", C.c_int32), ("npix_y", C.c_int32), ("pixel_cm", C.c_double),
                 ("incl_deg", C.c_double), ("pa_deg", C.c_double), ("phi_deg", C.c_double),
@@ -75,6 +90,8 @@ EXPORTS = [
     "pdgpu_image_plan_create", "pdgpu_image_plan_destroy", "pdgpu_image_plan_info",
     "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint",
     "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint", "pdgpu_mctherm_static",
+    "pdgpu_scat_plan_create", "pdgpu_scat_plan_destroy", "pdgpu_scat_plan_info",
+    "pdgpu_scat_plan_upload", "pdgpu_scat_run", "pdgpu_scat_plan_stats",
 ]
 
 
@@ -139,6 +156,19 @@ def lib(build_if_missing=True):
     L.pdgpu_mctherm_static.restype = i32
     L.pdgpu_mctherm_static.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
                                        C.POINTER(McOptions), vp, vp, vp, C.POINTER(McStats)]
+    L.pdgpu_scat_plan_create.restype = i32
+    L.pdgpu_scat_plan_create.argtypes = [C.POINTER(ModelDesc), i32, dp, i32, dp, dp,
+                                         C.POINTER(ScatOptions), C.POINTER(vp)]
+    L.pdgpu_scat_plan_destroy.restype = None
+    L.pdgpu_scat_plan_destroy.argtypes = [vp]
+    L.pdgpu_scat_plan_info.restype = i32
+    L.pdgpu_scat_plan_info.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_int64)]
+    L.pdgpu_scat_plan_upload.restype = i32
+    L.pdgpu_scat_plan_upload.argtypes = [vp, vp, sz, vp]
+    L.pdgpu_scat_run.restype = i32
+    L.pdgpu_scat_run.argtypes = [vp, vp, vp, vp, vp, sz, vp]
+    L.pdgpu_scat_plan_stats.restype = i32
+    L.pdgpu_scat_plan_stats.argtypes = [vp, vp, vp, C.POINTER(ScatStats)]
     d = C.c_double
     L.pdgpu_vis_dft.restype = i32
     L.pdgpu_vis_dft.argtypes = [i32, i32, d, d, d, d, vp, i32, vp, vp, vp, vp, vp]

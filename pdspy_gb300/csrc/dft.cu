@@ -8,8 +8,8 @@
 // (pdspy/interferometry/interpolate_model.py:11-57); a direct sum is exact at every uv
 // point and has a simple, exact adjoint.
 //
-// Forward: one thread per uv point, image tiles staged in shared memory and read by the
-// whole block.  Adjoint: one thread per pixel, uv tiles staged in shared memory.  Phases
+// Forward: four threads per uv point, image tiles staged in shared memory and read by the
+// whole block.  Adjoint: four threads per pixel, uv tiles staged in shared memory.  Phases
 // are formed in FP32 (|u x| of a few turns keeps the phase error ~1e-6 rad) and
 // evaluated with sincospif; sums accumulate in FP32 per tile and in FP64 across tiles.
 #include <cuda_runtime.h>
@@ -21,6 +21,14 @@
 namespace {
 
 constexpr int DFT_TILE = 512;
+// A block of 256 threads serves DFT_POINTS outputs (uv points forward, pixels adjoint);
+// the DFT_GROUPS warp pairs of the block split each staged tile by index modulo
+// DFT_GROUPS, so every warp reads one shared-memory entry per step (a broadcast) and the
+// group partial sums are added in a fixed order at the end: deterministic results and
+// four times the blocks of a thread-per-output launch.
+constexpr int DFT_GROUPS = 4;
+constexpr int DFT_POINTS = 64;
+static_assert(DFT_GROUPS * DFT_POINTS == 256, "one block of 256 threads");
 
 __global__ void __launch_bounds__(256) dft_forward_kernel(int nx, int ny, float x0, float dx,
                                                           float y0, float dy, const float* img,
@@ -30,7 +38,11 @@ __global__ void __launch_bounds__(256) dft_forward_kernel(int nx, int ny, float 
     __shared__ float s_f[DFT_TILE];
     __shared__ float s_x[DFT_TILE];
     __shared__ float s_y[DFT_TILE];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_re[DFT_GROUPS][DFT_POINTS];
+    __shared__ double s_im[DFT_GROUPS][DFT_POINTS];
+    const int j = threadIdx.x % DFT_POINTS;
+    const int g = threadIdx.x / DFT_POINTS;
+    const int k = blockIdx.x * DFT_POINTS + j;
     const float uk = (k < nuv) ? u[k] : 0.0f;
     const float vk = (k < nuv) ? v[k] : 0.0f;
     const int npix = nx * ny;
@@ -46,7 +58,7 @@ __global__ void __launch_bounds__(256) dft_forward_kernel(int nx, int ny, float 
         }
         __syncthreads();
         float tr = 0.0f, ti = 0.0f;
-        for (int i = 0; i < n; ++i) {
+        for (int i = g; i < n; i += DFT_GROUPS) {
             float f = s_f[i];
             if (f == 0.0f) continue;
             float ph = 2.0f * (uk * s_x[i] + vk * s_y[i]);
@@ -58,9 +70,17 @@ __global__ void __launch_bounds__(256) dft_forward_kernel(int nx, int ny, float 
         ar += tr;
         ai += ti;
     }
-    if (k < nuv) {
-        re[k] = ar;
-        im[k] = ai;
+    s_re[g][j] = ar;
+    s_im[g][j] = ai;
+    __syncthreads();
+    if (g == 0 && k < nuv) {
+        double r = s_re[0][j], q = s_im[0][j];
+        for (int h = 1; h < DFT_GROUPS; ++h) {
+            r += s_re[h][j];
+            q += s_im[h][j];
+        }
+        re[k] = r;
+        im[k] = q;
     }
 }
 
@@ -73,7 +93,10 @@ __global__ void __launch_bounds__(256) dft_adjoint_kernel(int nx, int ny, float 
     __shared__ float s_v[DFT_TILE];
     __shared__ float s_gr[DFT_TILE];
     __shared__ float s_gi[DFT_TILE];
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_acc[DFT_GROUPS][DFT_POINTS];
+    const int j = threadIdx.x % DFT_POINTS;
+    const int g = threadIdx.x / DFT_POINTS;
+    const int p = blockIdx.x * DFT_POINTS + j;
     const int npix = nx * ny;
     const float xp = x0 + (float)(p % nx) * dx;
     const float yp = y0 + (float)(p / nx) * dy;
@@ -89,7 +112,7 @@ __global__ void __launch_bounds__(256) dft_adjoint_kernel(int nx, int ny, float 
         }
         __syncthreads();
         float t = 0.0f;
-        for (int i = 0; i < n; ++i) {
+        for (int i = g; i < n; i += DFT_GROUPS) {
             float ph = 2.0f * (s_u[i] * xp + s_v[i] * yp);
             float sn, cs;
             sincospif(ph, &sn, &cs);
@@ -98,7 +121,13 @@ __global__ void __launch_bounds__(256) dft_adjoint_kernel(int nx, int ny, float 
         }
         acc += t;
     }
-    if (p < npix) gimg[p] = acc;
+    s_acc[g][j] = acc;
+    __syncthreads();
+    if (g == 0 && p < npix) {
+        double a = s_acc[0][j];
+        for (int h = 1; h < DFT_GROUPS; ++h) a += s_acc[h][j];
+        gimg[p] = a;
+    }
 }
 
 }  // namespace
@@ -110,9 +139,10 @@ pdgpu_status pdgpu_vis_dft(int32_t nx, int32_t ny, double x0_rad, double dx_rad,
                            const float* v, double* re, double* im, void* stream) {
     if (nx < 1 || ny < 1 || nuv < 1 || !image || !u || !v || !re || !im) return PDGPU_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    dft_forward_kernel<<<(nuv + 255) / 256, 256, 0, st>>>(nx, ny, (float)x0_rad, (float)dx_rad,
-                                                         (float)y0_rad, (float)dy_rad, image, nuv,
-                                                         u, v, re, im);
+    const int blocks = (nuv + DFT_POINTS - 1) / DFT_POINTS;
+    dft_forward_kernel<<<blocks, 256, 0, st>>>(nx, ny, (float)x0_rad, (float)dx_rad,
+                                               (float)y0_rad, (float)dy_rad, image, nuv, u, v,
+                                               re, im);
     return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
 }
 
@@ -124,9 +154,10 @@ pdgpu_status pdgpu_vis_dft_adjoint(int32_t nx, int32_t ny, double x0_rad, double
         return PDGPU_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     int npix = nx * ny;
-    dft_adjoint_kernel<<<(npix + 255) / 256, 256, 0, st>>>(nx, ny, (float)x0_rad, (float)dx_rad,
-                                                          (float)y0_rad, (float)dy_rad, nuv, u, v,
-                                                          grad_re, grad_im, grad_image);
+    const int blocks = (npix + DFT_POINTS - 1) / DFT_POINTS;
+    dft_adjoint_kernel<<<blocks, 256, 0, st>>>(nx, ny, (float)x0_rad, (float)dx_rad,
+                                               (float)y0_rad, (float)dy_rad, nuv, u, v, grad_re,
+                                               grad_im, grad_image);
     return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
 }
 

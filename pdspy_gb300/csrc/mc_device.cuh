@@ -62,6 +62,49 @@ __device__ __forceinline__ float mc_logf(float x) {
     return (float)e * 0.69314718f + lm;
 }
 
+// exp(-x) for x >= 0 (0 beyond x = 87): x = n ln2 + r with |r| <= ln2 / 2 (Cody & Waite's
+// two-part ln2, hi part with 8 trailing zero bits so n * hi is exact), e^-r by its Taylor
+// series to r^7 (truncation below 6e-9 relative), times 2^-n built from the exponent bits.
+__device__ __forceinline__ float mc_expm(float x) {
+    if (!(x < 87.0f)) return 0.0f;
+    int n = (int)(x * 1.44269504f + 0.5f);
+    float r = (x - (float)n * 0.693145751953125f) - (float)n * 1.42860677e-06f;
+    float p = -1.98412698e-04f;
+    p = p * r + 1.38888889e-03f;
+    p = p * r - 8.33333333e-03f;
+    p = p * r + 4.16666667e-02f;
+    p = p * r - 1.66666667e-01f;
+    p = p * r + 0.5f;
+    p = p * r - 1.0f;
+    p = p * r + 1.0f;
+    return p * __uint_as_float((uint32_t)(127 - n) << 23);
+}
+
+// (1 - exp(-x)) / x for x >= 0: its series to x^5 below 0.1 (truncation below 2e-10),
+// the difference above.
+__device__ __forceinline__ float mc_expm_frac(float x, float e) {
+    if (x < 0.1f) {
+        float p = -1.38888889e-03f;
+        p = p * x + 8.33333333e-03f;
+        p = p * x - 4.16666667e-02f;
+        p = p * x + 1.66666667e-01f;
+        p = p * x - 0.5f;
+        return p * x + 1.0f;
+    }
+    return (1.0f - e) / x;
+}
+
+// Cube root of x in (0, 1]: a first guess from the exponent bits (one third of the
+// biased exponent and mantissa, offset so the guess is within a few percent), then four
+// Newton steps y <- (2 y + x / y^2) / 3.
+__device__ __forceinline__ float mc_cbrt01(float x) {
+    uint32_t b = __float_as_uint(x);
+    float y = __uint_as_float(b / 3u + 709921077u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) y = (2.0f * y + x / (y * y)) * 0.333333343f;
+    return y;
+}
+
 // sin and cos of 2 pi u, u in (0,1): nearest quarter turn plus Taylor series of sin (to
 // x^9) and cos (to x^8) on |x| <= pi/4.
 __device__ __forceinline__ void mc_sincospif2(float u, float& sn, float& cs) {

@@ -10,9 +10,13 @@ integrates the formal solution.  Results land where the reference puts them:
 in arcsec and ``wave`` in cm, Model.py:566-572) and ``model.spectra[name]`` (a Spectrum
 with wavelengths in microns and fluxes in Jy at ``dpc``, Model.py:646-648).
 
-Emission is thermal: S = B_nu(T) sum_s rho_s kabs_s / alpha with alpha = sum_s rho_s
-(kabs_s + ksca_s); the Monte Carlo scattering source RADMC-3D adds for albedo > 0 is not
-included (at millimetre wavelengths the albedo of the configured dust is zero).
+The source function is S = [B_nu(T) sum_s rho_s kabs_s + J sum_s rho_s ksca_s] / alpha with
+alpha = sum_s rho_s (kabs_s + ksca_s): thermal emission plus, where the dust scatters,
+the isotropic scattering of the mean intensity J that the GPU scattering Monte Carlo
+(``scatter.ScatterPlan``) computes with ``nphot`` packets per wavelength, as RADMC-3D
+does before "radmc3d image" / "radmc3d spectrum" (nphot_scat / nphot_spec,
+mc_scat_maxtauabs; pdspy/radmc3d/write.py:33-38, :141-142).  ``scattering_mode_max=0``
+switches scattering off as in RADMC-3D.
 
 ``RayTrace`` is a ``torch.autograd.Function`` whose backward is the hand-written adjoint
 of the ray trace (``pdgpu_image_adjoint``).
@@ -71,15 +75,24 @@ def mean_temperature(rho, T):
     return (r * T).sum(0) / r.sum(0)
 
 
-def source_terms(rho, T, kabs, ksca, lam_um):
-    """(alpha, S) [nlam, ncell] from rho, T [nspec, ncell] and opacities [nspec, nlam]."""
+def thermal_emissivity(rho, T, kabs, lam_um):
+    """sum_s rho_s kabs_s B_nu(Tm) [nlam, ncell] (erg/s/cm^3/Hz/ster) at the density-weighted
+    mean temperature Tm pdspy writes for image mode."""
     nu = (C_LIGHT / (torch.as_tensor(lam_um, dtype=rho.dtype, device=rho.device) * 1.0e-4))
     Tm = mean_temperature(rho, T)
-    alpha = torch.einsum("sl,sc->lc", kabs + ksca, rho)
     jab = torch.einsum("sl,sc->lc", kabs, rho)
-    B = planck_nu(nu[:, None], Tm[None, :])
+    return planck_nu(nu[:, None], Tm[None, :]) * jab
+
+
+def source_terms(rho, T, kabs, ksca, lam_um, J=None):
+    """(alpha, S) [nlam, ncell] from rho, T [nspec, ncell] and opacities [nspec, nlam];
+    J [nlam, ncell] (the mean intensity) adds the isotropic scattering source."""
+    alpha = torch.einsum("sl,sc->lc", kabs + ksca, rho)
+    emis = thermal_emissivity(rho, T, kabs, lam_um)
+    if J is not None:
+        emis = emis + torch.einsum("sl,sc->lc", ksca, rho) * J
     safe = torch.where(alpha > 0, alpha, torch.ones_like(alpha))
-    S = torch.where(alpha > 0, B * jab / safe, torch.zeros_like(alpha))
+    S = torch.where(alpha > 0, emis / safe, torch.zeros_like(alpha))
     return alpha, S
 
 
@@ -210,8 +223,8 @@ class RayTrace(torch.autograd.Function):
         return ga.to(ctx.dtypes[0]), gs.to(ctx.dtypes[1]), None
 
 
-def model_sources(model, lam_um, device):
-    """(alpha, S) float32 on the device for the model's densities and temperatures."""
+def model_state(model, device):
+    """(rho, T) float64 [nspec, ncell] on the device."""
     g = model.grid
     if len(g.temperature) != len(g.density):
         raise ValueError("run_image needs grid.temperature (run run_thermal first)")
@@ -219,10 +232,34 @@ def model_sources(model, lam_um, device):
                                     for d in g.density]), device=device)
     T = torch.as_tensor(np.stack([np.asarray(t, dtype=np.float64).reshape(-1)
                                   for t in g.temperature]), device=device)
+    return rho, T
+
+
+def model_sources(model, lam_um, device, nphot_scat=0, scattering=True,
+                  maxtauabs=30.0, seed=0):
+    """(alpha, S) float32 on the device for the model's densities and temperatures.  With
+    nphot_scat > 0 and scattering dust the scattering source is computed by the GPU
+    scattering Monte Carlo; scattering=False drops scattering altogether."""
+    from .scatter import ScatterPlan
+    g = model.grid
+    rho, T = model_state(model, device)
     ka, ks = opacities(g, lam_um)
-    alpha, S = source_terms(rho, T, torch.as_tensor(ka, device=device),
-                            torch.as_tensor(ks, device=device), lam_um)
+    if not scattering:
+        ks = np.zeros_like(ks)
+    kat = torch.as_tensor(ka, device=device)
+    J = None
+    if nphot_scat > 0 and np.any(ks > 0):
+        plan = ScatterPlan(g, lam_um, ka, ks, int(nphot_scat), maxtauabs=maxtauabs, seed=seed,
+                           device=device)
+        J = plan.run(rho, thermal_emissivity(rho, T, kat, lam_um))
+    alpha, S = source_terms(rho, T, kat, torch.as_tensor(ks, device=device), lam_um, J=J)
     return alpha.to(torch.float32).contiguous(), S.to(torch.float32).contiguous()
+
+
+def _scat_keywords(keywords):
+    from .scatter import maxtauabs_of, scattering_enabled
+    return dict(scattering=scattering_enabled(keywords), maxtauabs=maxtauabs_of(keywords),
+                seed=int(keywords.get("iseed", 0) or 0))
 
 
 def run_image(model, name=None, nphot=1e6, npix=256, pixelsize=1.0, lam="1300",
@@ -235,7 +272,7 @@ def run_image(model, name=None, nphot=1e6, npix=256, pixelsize=1.0, lam="1300",
     plan = ImagePlan(model.grid, npix, pixel_cm, lam_um, incl=incl, pa=pa, phi=phi,
                      nostar=nostar, max_refine=max_refine, refine_factor=refine_factor,
                      device=dev)
-    alpha, S = model_sources(model, lam_um, dev)
+    alpha, S = model_sources(model, lam_um, dev, nphot_scat=int(nphot), **_scat_keywords(keywords))
     inten = plan.run(alpha, S).cpu().numpy()              # [nlam, ny, nx] at 1 pc
     omega = (pixel_cm / (dpc * pc)) ** 2
     image = np.ascontiguousarray(np.transpose(inten, (1, 2, 0))[:, :, :, None]) / Jy * omega
@@ -256,7 +293,7 @@ def run_sed(model, name=None, nphot=1e6, incl=0, pa=0, phi=0, dpc=1, loadlambda=
     pixel_cm = 2.02 * r[-1] / npix
     plan = ImagePlan(g, npix, pixel_cm, lam_um, incl=incl, pa=pa, phi=phi, nostar=False,
                      max_refine=max_refine, refine_factor=refine_factor, device=dev)
-    alpha, S = model_sources(model, lam_um, dev)
+    alpha, S = model_sources(model, lam_um, dev, nphot_scat=int(nphot), **_scat_keywords(keywords))
     inten = plan.run(alpha, S)
     omega = (pixel_cm / pc) ** 2
     flux_1pc = (inten.sum(dim=(1, 2)) * omega).cpu().numpy()   # erg/s/cm^2/Hz at 1 pc

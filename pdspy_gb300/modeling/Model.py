@@ -1,7 +1,8 @@
 """Generic model; mirrors pdspy/modeling/Model.py with a "gb300" code path.
 
-``run_thermal``, ``run_image`` and ``run_sed`` keep the reference's signatures and
-string dispatch on ``code`` (Model.py:69-72, :345-348, :600-603).  ``code="gb300"`` (the
+``run_thermal``, ``run_scattering``, ``run_image`` and ``run_sed`` keep the reference's
+signatures and string dispatch on ``code`` (Model.py:69-72, :275-278, :345-348,
+:600-603).  ``code="gb300"`` (the
 default here) runs the CUDA backend; "radmc3d" and "hyperion" name external programs
 that are not part of this package and raise NotImplementedError.
 """
@@ -22,6 +23,12 @@ class Model:
         if code == "gb300":
             from ..thermal import run_thermal
             return run_thermal(self, nphot=nphot, **keywords)
+        raise NotImplementedError("code=%r is an external program; use code='gb300'" % code)
+
+    def run_scattering(self, nphot=1e6, code="gb300", **keywords):
+        if code == "gb300":
+            from ..scatter import run_scattering
+            return run_scattering(self, nphot=nphot, **keywords)
         raise NotImplementedError("code=%r is an external program; use code='gb300'" % code)
 
     def run_image(self, name=None, nphot=1e6, code="gb300", **keywords):

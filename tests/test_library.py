@@ -27,7 +27,7 @@ def test_library_exports_declared_symbols():
 
 def test_abi_version_and_status_strings():
     L = _lib.lib()
-    assert L.pdgpu_abi_version() == 3
+    assert L.pdgpu_abi_version() == 4
     assert L.pdgpu_status_string(2) == b"time limit reached"
 
 
