@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-reps", type=int, default=10)
+    ap.add_argument("--no-scattering", action="store_true")
     ap.add_argument("--cpu-models", type=int, default=8)
     ap.add_argument("--cpu-packets", type=int, default=100000)
     ap.add_argument("--timelimit", type=float, default=1800.0,
@@ -198,6 +199,57 @@ def adjoint_rate(dev, seed, reps):
             "grad_params": [float(x) for x in gp.cpu()]}
 
 
+def scattering_rate(dev, seed, reps=5, cpu=True):
+    """Scattering Monte Carlo of an SED (the scattering-source workload): disk plus Ulrich
+    envelope on 256 x 256 cells, 100 wavelengths log-spaced over 0.1-1e4 microns, 1e4
+    packets per wavelength and mc_scat_maxtauabs = 5 (pdspy's run_sed call in
+    run_disk_model.py), photons from the star and the dust (analytic temperatures).
+    GPU packets/s by CUDA events; the CPU restatement on every tenth wavelength."""
+    import torch
+    from pdspy_gb300 import image, scatter, thermal, workloads
+    m = workloads.disk_envelope(nr=256, ntheta=256)
+    g = m.grid
+    rr = np.meshgrid(g.r, g.theta, g.phi, indexing="ij")[0]
+    g.temperature = [np.maximum(150.0 * rr ** -0.5, 10.0)] * len(g.density)
+    lam = np.logspace(-1, 4, 100)
+    nphot, mt = 10000, 5.0
+    rho, T = image.model_state(m, dev)
+    ka, ks = image.opacities(g, lam)
+    emis = image.thermal_emissivity(rho, T, torch.as_tensor(ka, device=dev), lam)
+    plan = scatter.ScatterPlan(g, lam, ka, ks, nphot, maxtauabs=mt, seed=seed, device=dev)
+    for _ in range(3):
+        plan.run(rho, emis)
+    torch.cuda.synchronize(dev)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        plan.run(rho, emis)
+    b.record()
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    st = plan.stats()
+    out = {"gpu_packets_per_s": st["packets"] / (ms / 1e3), "ms_per_sed": ms,
+           "packets_per_sed": st["packets"], "scatterings_per_sed": st["scatterings"],
+           "config": "disk+envelope 256x256 cells, 100 wavelengths 0.1-1e4 um, 1e4 "
+                     "packets each, maxtauabs 5, star + dust sources"}
+    if cpu:
+        from oracle import orc
+        r, t, p = thermal.grid_arrays(g)
+        radius, temp = thermal._stars(g)
+        sel = np.arange(0, 100, 10)
+        t0 = time.perf_counter()
+        o = orc.mcscat(r, t, p, rho.float().cpu().numpy(), lam[sel], ka[:, sel], ks[:, sel],
+                       radius, temp, nphot, emis=emis[sel].cpu().numpy(), maxtauabs=mt,
+                       seed=seed)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": o["stats"]["packets"] / dt, "unit": "packets/s",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": "every tenth wavelength (%d packets, %.2f s)" %
+                                         (o["stats"]["packets"], dt)}
+    return out
+
+
 def workload_name(args):
     if args.workload == "plain":
         return "plain-disk-100x100-%g-packets-mrw" % args.packets
@@ -339,6 +391,10 @@ def main():
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_rate(dev, args.seed, args.adjoint_reps)
 
+    scat = None
+    if rank == 0 and not args.no_scattering:
+        scat = scattering_rate(dev, args.seed, cpu=not args.no_cpu)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_sample(models, args, os.cpu_count())
@@ -364,6 +420,7 @@ def main():
                            "geometry": "double-single (FP32 pipe); FP64 energy->temperature",
                            "parallelism": "replicas: independent walker batches per GPU"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adj,
+                "scattering": scat,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
                                             "parked", "drained", "killed", "late_units")},

@@ -268,6 +268,25 @@ pdgpu_status pdgpu_vis_dft_adjoint(int32_t nx, int32_t ny, double x0_rad, double
                                    const float* v, const double* grad_re,
                                    const double* grad_im, double* grad_image, void* stream);
 
+/* Gridded sampling (galario's sampleImage method, pdspy/interferometry/interpolate_model.py:
+ * 11-57): grid (device complex64 [n][n], interleaved re/im) is the 2-D FFT
+ * G[l][k] = sum_j,i F[j][i] exp(-2 pi i (k i + l j) / n) of an n x n (zero-padded, n even)
+ * image whose centre pixel (n/2, n/2) sits at (xc, yc) radians; du = 1 / (n dx) and
+ * dv = 1 / (n dy).  re/im (device double [nuv]) = bilinear interpolation of
+ * (-1)^(k+l) G at (u / du, v / dv) times exp(-2 pi i (u xc + v yc)): the sum of
+ * pdgpu_vis_dft up to the interpolation error.  Points with |u / du| or |v / dv| >= n/2 - 1
+ * give NaN. */
+pdgpu_status pdgpu_vis_grid_sample(int32_t n, const float* grid, double du, double dv, double xc,
+                                   double yc, int32_t nuv, const float* u, const float* v,
+                                   double* re, double* im, void* stream);
+/* Adjoint of pdgpu_vis_grid_sample: accumulates into grad_grid (device complex128 [n][n],
+ * zeroed by the caller) the grid-side gradient H; the image gradient is
+ * Re(FFT2(H)) over the image's pixels.  No counterpart in the reference. */
+pdgpu_status pdgpu_vis_grid_sample_adjoint(int32_t n, double du, double dv, double xc, double yc,
+                                           int32_t nuv, const float* u, const float* v,
+                                           const double* grad_re, const double* grad_im,
+                                           double* grad_grid, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Monte Carlo scattering source (images and spectra at albedo > 0)           */
 /* ------------------------------------------------------------------------- */

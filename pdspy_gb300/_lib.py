@@ -92,6 +92,7 @@ EXPORTS = [
     "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint", "pdgpu_mctherm_static",
     "pdgpu_scat_plan_create", "pdgpu_scat_plan_destroy", "pdgpu_scat_plan_info",
     "pdgpu_scat_plan_upload", "pdgpu_scat_run", "pdgpu_scat_plan_stats",
+    "pdgpu_vis_grid_sample", "pdgpu_vis_grid_sample_adjoint",
 ]
 
 
@@ -174,6 +175,10 @@ def lib(build_if_missing=True):
     L.pdgpu_vis_dft.argtypes = [i32, i32, d, d, d, d, vp, i32, vp, vp, vp, vp, vp]
     L.pdgpu_vis_dft_adjoint.restype = i32
     L.pdgpu_vis_dft_adjoint.argtypes = [i32, i32, d, d, d, d, i32, vp, vp, vp, vp, vp, vp]
+    L.pdgpu_vis_grid_sample.restype = i32
+    L.pdgpu_vis_grid_sample.argtypes = [i32, vp, d, d, d, d, i32, vp, vp, vp, vp, vp]
+    L.pdgpu_vis_grid_sample_adjoint.restype = i32
+    L.pdgpu_vis_grid_sample_adjoint.argtypes = [i32, d, d, d, d, i32, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

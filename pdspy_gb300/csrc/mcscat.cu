@@ -338,7 +338,7 @@ __device__ __forceinline__ long long sc_warp_sum(long long v) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) sc_transport_kernel(ScParams P) {
+__global__ void __launch_bounds__(256, 3) sc_transport_kernel(ScParams P) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     ScCnt cnt = {0, 0, 0, 0, 0, 0};
