@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-reps", type=int, default=10)
     ap.add_argument("--no-scattering", action="store_true")
+    ap.add_argument("--lnprob-walkers", type=int, default=0,
+                    help="also time the batched MCMC lnprob of this many walkers (0: off)")
+    ap.add_argument("--lnprob-packets", type=int, default=100000)
     ap.add_argument("--cpu-models", type=int, default=8)
     ap.add_argument("--cpu-packets", type=int, default=100000)
     ap.add_argument("--timelimit", type=float, default=1800.0,
@@ -250,6 +253,36 @@ def scattering_rate(dev, seed, reps=5, cpu=True):
     return out
 
 
+def lnprob_rate(dev, seed, nwalkers, nphot):
+    """Batched lnprob of an emcee ensemble (the power-law disk family of pdspy's
+    run_disk_model.py): walkers with log-uniform disk masses 1e-5..1e-3 Msun, h_0 in
+    [0.05, 0.15], inclination in [20, 70] deg on run_disk_model's 99 x 100 grid; one
+    visibility set of 20,000 points at 1.3 mm, 256^2-pixel images of 0.02 arcsec.  One
+    evaluation = device densities, one batched thermal launch, an image and an FFT
+    sampling per walker."""
+    import torch
+    from pdspy_gb300 import fitting, vis
+    P = fitting.base_parameters()
+    for k in ("h_0", "i", "logM_disk"):
+        P[k]["fixed"] = False
+    P["logR_disk"]["value"] = 1.5
+    rng = np.random.default_rng(seed)
+    walkers = np.stack([rng.uniform(0.05, 0.15, nwalkers), rng.uniform(20, 70, nwalkers),
+                        rng.uniform(-5, -3, nwalkers)], axis=1)
+    u, v = vis.synthetic_uv(20000, seed=seed, bmin_klam=10, bmax_klam=1500)
+    data = vis.UVData(u, v, np.zeros(u.size), np.zeros(u.size), np.full(u.size, 1e6),
+                      freq=2.99792458e10 / 0.13)
+    sets = [dict(data=data, npix=256, pixelsize=0.02)]
+    fitting.lnprob_batched(walkers[:2], sets, P, nphot=10000, device=dev, seed=seed)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    lp = fitting.lnprob_batched(walkers, sets, P, nphot=nphot, device=dev, seed=seed)
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    return {"walkers": nwalkers, "packets_per_walker": nphot, "s": dt,
+            "lnprob_per_s": nwalkers / dt, "finite": int(np.isfinite(lp).sum())}
+
+
 def workload_name(args):
     if args.workload == "plain":
         return "plain-disk-100x100-%g-packets-mrw" % args.packets
@@ -395,6 +428,10 @@ def main():
     if rank == 0 and not args.no_scattering:
         scat = scattering_rate(dev, args.seed, cpu=not args.no_cpu)
 
+    lnp = None
+    if rank == 0 and args.lnprob_walkers > 0:
+        lnp = lnprob_rate(dev, args.seed, args.lnprob_walkers, args.lnprob_packets)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_sample(models, args, os.cpu_count())
@@ -420,7 +457,7 @@ def main():
                            "geometry": "double-single (FP32 pipe); FP64 energy->temperature",
                            "parallelism": "replicas: independent walker batches per GPU"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adj,
-                "scattering": scat,
+                "scattering": scat, "lnprob": lnp,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
                                             "parked", "drained", "killed", "late_units")},

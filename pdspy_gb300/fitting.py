@@ -1,0 +1,210 @@
+"""Batched log-probability of an MCMC ensemble on one GPU.
+
+pdspy fits a model by emcee: ``lnprob`` (pdspy/utils/emcee.py:183-203) = ``lnprior``
+(:64-150) + ``lnlike`` (:6-61), evaluated one walker at a time, each walker running
+``run_disk_model`` (pdspy/modeling/run_disk_model.py: parameters :39-56, model set-up
+:112-205, the RADMC-3D thermal run :251-255, images and galario sampling per visibility
+set :285-330) in its own process (bin/disk_model_emcee3.py:177-184 farms the walkers
+over an MPI pool).  ``lnprob_batched`` evaluates a whole ensemble in one go:
+
+  1. every walker's parameters are resolved as run_disk_model does and its prior checked;
+  2. the models of the walkers with a finite prior are built with the device density
+     builders (``builders``) on run_disk_model's grid (set_spherical_grid(R_in, R_grid,
+     100, 101, 2): 99 x 100 x 1 cells, theta mirrored, R_grid = R_env with an envelope,
+     else 5 R_disk);
+  3. ONE batched thermal launch (``thermal.run_thermal_batched``) computes all their
+     temperatures with run_disk_model's settings (1e6 packets, MRW gamma 2, tauthres 10,
+     count trigger 100); a walker whose run times out gets -inf, as run_disk_model's
+     TimeoutExpired branch returns 0 and lnlike then -inf;
+  4. per walker and visibility set: the image at the set's wavelength (``image``), scaled
+     by flux_unc, sampled at the data's (u, v) by the gridded FFT (``vis.VisFFT``,
+     galario's method) with the (x0, y0) offset, and lnlike's visibility term.
+
+Scope: the "truncated" power-law disk with an optional "ulrich-extended" envelope (its
+centrifugal radius = R_disk, as YSOModel does unless rcent_ne_rdisk), the visibility
+likelihood (lnlike's image and SED terms need data products outside this path), and one
+dust model for disk and envelope (pdspy's DustGenerator tables are not available).
+"""
+import subprocess
+
+import numpy as np
+import torch
+
+from . import builders, image, thermal, vis
+from .constants import arcsec, c as C_LIGHT
+from .modeling import Model, Star
+
+# run_disk_model's thermal settings (run_disk_model.py:251-255)
+THERMAL = dict(modified_random_walk=True, mrw_gamma=2, mrw_tauthres=10, mrw_count_trigger=100)
+
+
+def base_parameters():
+    """pdspy's default parameter table (pdspy/modeling/base_parameters.py) for the keys of
+    this model family: every entry fixed at pdspy's default value and limits."""
+    def e(v, lo, hi, **kw):
+        return dict(fixed=True, value=v, limits=[lo, hi], **kw)
+    return {
+        "logM_star": e(0.0, -1., 1.), "T_star": e(4000., 500., 10000.),
+        "logL_star": e(0.0, -1., 2.), "disk_type": e("truncated", 0., 0.),
+        "logM_disk": e(-4., -10., -2.5), "logR_in": e(-1., -1., 4.), "logR_disk": e(2., 0., 4.),
+        "h_0": e(0.1, 0.01, 0.5), "gamma": e(1.0, -0.5, 2.0), "beta": e(1.0, 0.5, 1.5),
+        "envelope_type": e("none", 0., 0.), "logM_env": e(-3., -10., -2.),
+        "logR_env": e(3., 2., 5.), "logR_c": e("logR_disk", -1., 4.), "f_cav": e(0.5, 0., 1.),
+        "ksi": e(1.0, 0.5, 1.5), "theta_open": e("45", 0., 90.), "zoffset": e(1, 0., 5.),
+        "i": e(45., 0., 180.), "pa": e(0., 0., 360.), "x0": e(0., -0.1, 0.1),
+        "y0": e(0., -0.1, 0.1), "dpc": e(140., 1., 1e6, prior="box", sigma=0.),
+        "flux_unc1": e(1., 0.5, 1.5, prior="box", sigma=0.),
+    }
+
+
+def resolve(params, parameters):
+    """run_disk_model's parameter dictionary (run_disk_model.py:39-56): fixed values (or
+    the value of the parameter they name), free values from ``params``, 10**x for every
+    "log" key, alpha = gamma + beta."""
+    p = {}
+    for key in parameters:
+        if parameters[key]["fixed"]:
+            v = parameters[key]["value"]
+            if isinstance(v, str) and v in parameters:
+                v = parameters[v]["value"] if parameters[v]["fixed"] else params[v]
+        else:
+            v = params[key]
+        p[key] = v
+        if key[:3] == "log":
+            p[key[3:]] = 10.0 ** float(v)
+    p["alpha"] = p["gamma"] + p["beta"]
+    return p
+
+
+def free_keys(parameters):
+    return [k for k in sorted(parameters) if not parameters[k]["fixed"]]
+
+
+def lnprior(params, parameters, priors, nvis):
+    """pdspy's lnprior (utils/emcee.py:64-150) for the parameters this family has."""
+    for key in parameters:
+        if not parameters[key]["fixed"]:
+            lo, hi = parameters[key]["limits"]
+            if not lo <= params[key] <= hi:
+                return -np.inf
+
+    def val(k):
+        return params[k] if k in params else parameters[k]["value"]
+
+    R_in, R_disk, R_env = (10.0 ** float(val(k)) for k in ("logR_in", "logR_disk", "logR_env"))
+    if not R_in <= R_disk <= R_env:
+        return -np.inf
+    if "logR_env" in params and "logM_env" in params:
+        if params["logR_env"] < 0.5 * params["logM_env"] + 4.0:
+            return -np.inf
+    lp = 0.0
+    for i in range(nvis):
+        k = "flux_unc%d" % (i + 1)
+        if k in parameters and not parameters[k]["fixed"] and \
+                parameters[k].get("prior") == "gaussian":
+            lp += -0.5 * (params[k] - parameters[k]["value"]) ** 2 / parameters[k]["sigma"] ** 2
+    if "dpc" in parameters and not parameters["dpc"]["fixed"]:
+        if "parallax" in priors:
+            plx = 1.0 / params["dpc"] * 1000
+            lp += -0.5 * (plx - priors["parallax"]["value"]) ** 2 / priors["parallax"]["sigma"] ** 2
+        elif "dpc" in priors:
+            lp += -0.5 * (params["dpc"] - priors["dpc"]["value"]) ** 2 / priors["dpc"]["sigma"] ** 2
+    return lp
+
+
+def build_model(p, dust, lam_um, device):
+    """The walker's Model: star, run_disk_model's grid, disk (+ envelope) densities from
+    the device builders."""
+    m = Model()
+    m.grid.add_star(Star(mass=p.get("M_star", 1.0), luminosity=p["L_star"],
+                         temperature=p["T_star"]))
+    env = p.get("envelope_type", "none") == "ulrich-extended"
+    R_grid = p["R_env"] if env else 5 * p["R_disk"]
+    r = np.logspace(np.log10(p["R_in"]), np.log10(R_grid), 100)
+    th = np.linspace(0.0, np.pi / 2, 101)
+    ph = np.linspace(0.0, 2 * np.pi, 2)
+    m.grid.set_spherical_grid(r, th, ph)
+    m.grid.lam = lam_um
+    g = m.grid
+    rho = builders.disk_density(g.r, g.theta, g.phi, p["M_disk"], p["R_in"], p["R_disk"],
+                                p["alpha"], p["h_0"], p["beta"], device=device)
+    g.add_density(rho.cpu().numpy(), dust)
+    if env:
+        rho = builders.ulrich_envelope_density(g.r, g.theta, g.phi, p["M_env"], p["R_in"],
+                                               p["R_env"], p["R_disk"], p["ksi"], p["f_cav"],
+                                               float(p["theta_open"]), p["zoffset"],
+                                               device=device)
+        g.add_density(rho.cpu().numpy(), dust)
+    return m
+
+
+def _lnlike_vis(re, im, data):
+    """lnlike's visibility term (utils/emcee.py:31-43), numerically as pdspy writes it."""
+    w = data.weights
+    good = w > 0
+    norm = np.sum(np.log(w[good] / (2 * np.pi)))
+    return (-0.5 * np.sum((data.real - re) ** 2 * w) - norm +
+            -0.5 * np.sum((data.imag - im) ** 2 * w) - norm)
+
+
+def model_visibilities(m, p, vis_set, device, pad=2, nphot_image=1e5):
+    """Model visibilities (re, im) of walker m for one visibility set: run_image at the
+    set's wavelength (npix, pixelsize, incl i, pa, dpc), times flux_unc, sampled with the
+    (x0, y0) offset."""
+    data = vis_set["data"]
+    lam_um = C_LIGHT / np.atleast_1d(data.freq)[0] / 1.0e-4
+    npix, pixelsize = int(vis_set["npix"]), float(vis_set["pixelsize"])
+    img = image.run_image(m, name="vis", nphot=nphot_image, npix=npix, pixelsize=pixelsize,
+                          lam=[lam_um], incl=p["i"], pa=p["pa"], dpc=p["dpc"])
+    scale = float(p.get("flux_unc%d" % vis_set["index"], 1.0))
+    plane = torch.as_tensor(img.image[:, :, 0, 0] * scale, dtype=torch.float32, device=device)
+    geo = vis.pixel_grid(npix, pixelsize)
+    geo = (geo[0] + float(p.get("x0", 0.0)) * arcsec, geo[1],
+           geo[2] + float(p.get("y0", 0.0)) * arcsec, geo[3])
+    u = torch.as_tensor(data.u, dtype=torch.float32, device=device)
+    v = torch.as_tensor(data.v, dtype=torch.float32, device=device)
+    re, im = vis.VisFFT.apply(plane, u, v, geo, pad)
+    return re.cpu().numpy(), im.cpu().numpy()
+
+
+def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=None,
+                   nphot=1e6, device=None, pad=2, timelimit=3600.0, seed=0):
+    """lnprob of every walker (rows of P, the free parameters in sorted key order as
+    pdspy's lnprob orders them) with one batched thermal launch; returns float64 [nwalker].
+
+    visibilities: list of dicts with "data" (vis.UVData plus ``freq``), "npix" and
+    "pixelsize" (arcsec), one per visibility set (pdspy's visibilities["data"][j],
+    ["npix"][j], ["pixelsize"][j])."""
+    from .workloads import analytic_dust, lam_grid
+    priors = priors or {}
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    lam_um = lam_grid() if lam_um is None else lam_um
+    dust = analytic_dust(lam_um) if dust is None else dust
+    keys = free_keys(parameters)
+    out = np.full(len(P), -np.inf)
+    live, models, res, lps = [], [], [], []
+    for w, row in enumerate(P):
+        params = dict(zip(keys, [float(x) for x in row]))
+        lp = lnprior(params, parameters, priors, len(visibilities))
+        if not np.isfinite(lp):
+            continue
+        p = resolve(params, parameters)
+        live.append(w)
+        models.append(build_model(p, dust, lam_um, dev))
+        res.append(p)
+        lps.append(lp)
+    if not models:
+        return out
+    try:
+        thermal.run_thermal_batched(models, nphot=nphot, iseed=seed, timelimit=timelimit,
+                                    **THERMAL)
+    except subprocess.TimeoutExpired:
+        return out
+    for w, m, p, lp in zip(live, models, res, lps):
+        ll = 0.0
+        for j, vs in enumerate(visibilities):
+            vs = dict(vs, index=j + 1)
+            re, im = model_visibilities(m, p, vs, dev, pad=pad)
+            ll += _lnlike_vis(re, im, vs["data"])
+        out[w] = lp + ll
+    return out

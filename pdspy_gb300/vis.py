@@ -23,14 +23,16 @@ from .constants import arcsec
 
 
 class UVData:
-    """Visibility data: u, v in wavelengths; real, imag in Jy; weights 1/sigma^2."""
+    """Visibility data: u, v in wavelengths; real, imag in Jy; weights 1/sigma^2; freq in
+    Hz (optional)."""
 
-    def __init__(self, u, v, real, imag, weights):
+    def __init__(self, u, v, real, imag, weights, freq=None):
         self.u = np.asarray(u, dtype=np.float64)
         self.v = np.asarray(v, dtype=np.float64)
         self.real = np.asarray(real, dtype=np.float64)
         self.imag = np.asarray(imag, dtype=np.float64)
         self.weights = np.asarray(weights, dtype=np.float64)
+        self.freq = None if freq is None else np.atleast_1d(np.asarray(freq, dtype=np.float64))
 
 
 def synthetic_uv(n=20000, seed=0, bmin_klam=10.0, bmax_klam=2000.0):

@@ -1,0 +1,39 @@
+"""Parameter resolution, priors and model set-up of the batched lnprob (CPU): pdspy's
+run_disk_model.py:39-56 and utils/emcee.py:64-150."""
+import numpy as np
+import torch
+
+from pdspy_gb300 import fitting
+from tests.test_fitting_gpu import parameters
+
+
+def test_resolve_follows_run_disk_model():
+    P = parameters()
+    P["logR_c"] = {"fixed": True, "value": "logR_disk", "limits": [-1., 4.]}
+    p = fitting.resolve({"h_0": 0.1, "i": 40.0, "logM_disk": -3.0}, P)
+    assert p["M_disk"] == 10.0 ** -3.0 and p["R_disk"] == 10.0 ** 1.5
+    assert p["logR_c"] == 1.5 and p["R_c"] == 10.0 ** 1.5      # a fixed value naming a key
+    assert p["alpha"] == p["gamma"] + p["beta"]
+    assert p["theta_open"] == "45"
+
+
+def test_lnprior_radii_and_density_checks():
+    P = parameters()
+    assert fitting.lnprior({"h_0": 0.1, "i": 40.0, "logM_disk": -3.0}, P, {}, 1) == 0.0
+    assert fitting.lnprior({"h_0": 0.6, "i": 40.0, "logM_disk": -3.0}, P, {}, 1) == -np.inf
+    Q = dict(P, logR_disk={"fixed": True, "value": 3.5, "limits": [0., 4.]})
+    assert fitting.lnprior({"h_0": 0.1, "i": 40.0, "logM_disk": -3.0}, Q, {}, 1) == -np.inf
+
+
+def test_build_model_grid_and_densities():
+    P = parameters()
+    P["envelope_type"] = {"fixed": True, "value": "ulrich-extended", "limits": [0., 0.]}
+    p = fitting.resolve({"h_0": 0.1, "i": 40.0, "logM_disk": -3.0}, P)
+    from pdspy_gb300.workloads import analytic_dust, lam_grid
+    lam = lam_grid()
+    m = fitting.build_model(p, analytic_dust(lam), lam, torch.device("cpu"))
+    g = m.grid
+    assert len(g.w1) == 100 and len(g.w2) == 101 and len(g.w3) == 2
+    assert np.isclose(g.w1[-1], p["R_env"]) and np.isclose(g.w2[-1], np.pi / 2)
+    assert len(g.density) == 2 and g.density[0].shape == (99, 100, 1)
+    assert np.all(g.density[1] >= 0) and g.density[1].max() > 0
