@@ -283,6 +283,42 @@ def lnprob_rate(dev, seed, nwalkers, nphot):
             "lnprob_per_s": nwalkers / dt, "finite": int(np.isfinite(lp).sum())}
 
 
+def vis_rate(dev, seed):
+    """Visibility sampling of a 1024^2 image (0.01 arcsec pixels) at 1e5 uv points up to
+    5000 klambda: the gridded FFT path (pad 2, cuFFT + bilinear sampling) against the
+    direct sum, both on the GPU; forward only."""
+    import torch
+    from pdspy_gb300 import vis
+    n, nuv = 1024, 100000
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) - n // 2) * 0.01
+    img = np.exp(-0.5 * (x[None, :] ** 2 + x[:, None] ** 2) / 0.3 ** 2)
+    img = torch.as_tensor(img, dtype=torch.float32, device=dev)
+    u, v = vis.synthetic_uv(nuv, seed=seed, bmin_klam=10, bmax_klam=5000)
+    u = torch.as_tensor(u, dtype=torch.float32, device=dev)
+    v = torch.as_tensor(v, dtype=torch.float32, device=dev)
+    geo = vis.pixel_grid(n, 0.01)
+    out = {"npix": n, "points": nuv, "pad": 2}
+    for name, fn in (("fft", lambda: vis.VisFFT.apply(img, u, v, geo, 2)),
+                     ("dft", lambda: vis.VisDFT.apply(img, u, v, geo))):
+        fn()
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            re, im = fn()
+        b.record()
+        torch.cuda.synchronize(dev)
+        out[name + "_ms"] = a.elapsed_time(b) / 3
+        out[name] = (re, im)
+    re_f, im_f = out.pop("fft")
+    re_d, im_d = out.pop("dft")
+    scale = float(torch.sqrt(re_d ** 2 + im_d ** 2).max())
+    out["max_abs_diff_rel"] = float(torch.maximum((re_f - re_d).abs(), (im_f - im_d).abs()).max()) / scale
+    return out
+
+
 def workload_name(args):
     if args.workload == "plain":
         return "plain-disk-100x100-%g-packets-mrw" % args.packets
@@ -428,6 +464,10 @@ def main():
     if rank == 0 and not args.no_scattering:
         scat = scattering_rate(dev, args.seed, cpu=not args.no_cpu)
 
+    vrate = None
+    if rank == 0 and not args.no_adjoint:
+        vrate = vis_rate(dev, args.seed)
+
     lnp = None
     if rank == 0 and args.lnprob_walkers > 0:
         lnp = lnprob_rate(dev, args.seed, args.lnprob_walkers, args.lnprob_packets)
@@ -457,7 +497,7 @@ def main():
                            "geometry": "double-single (FP32 pipe); FP64 energy->temperature",
                            "parallelism": "replicas: independent walker batches per GPU"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adj,
-                "scattering": scat, "lnprob": lnp,
+                "scattering": scat, "lnprob": lnp, "visibility_sampling": vrate,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
                                             "parked", "drained", "killed", "late_units")},
