@@ -335,6 +335,17 @@ struct LanePol {
     __device__ __forceinline__ void remember(int, int, int, int, float) {}
     __device__ __forceinline__ float cached_value(int) const { return 0.0f; }
     __device__ __forceinline__ bool leader() const { return true; }
+    // densities of cell c (rho0 = the model's [spec][cell] block)
+    template <int NS>
+    __device__ __forceinline__ void density(const float* rho0, int ncell, int, int c, float* rh) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) rh[s] = __ldg(rho0 + (int64_t)s * ncell + c);
+    }
+    // snapshot (q_lo, q_span) of species s in cell c (q0 = the epoch's [spec][cell] block)
+    template <int NS>
+    __device__ __forceinline__ float2 snap(const float2* q0, int ncell, int, int c, int, int s) {
+        return q0[(int64_t)s * ncell + c];
+    }
 };
 
 struct WarpPol {
@@ -438,6 +449,36 @@ struct WarpPol {
     }
     __device__ __forceinline__ float cached_value(int k) const { return cval[k]; }
     __device__ __forceinline__ bool leader() const { return lane == 0; }
+    // densities and snapshots of the packet's cell, reloaded when the cell changes
+    int dm = -1, dc = -1, qm = -1, qc = -1, qe = -1;
+    float drho[MC_MAX_SPEC];
+    float2 dq[MC_MAX_SPEC];
+    template <int NS>
+    __device__ __forceinline__ void density(const float* rho0, int ncell, int m, int c, float* rh) {
+        if (m != dm || c != dc) {
+#pragma unroll
+            for (int s = 0; s < NS; ++s) drho[s] = __ldg(rho0 + (int64_t)s * ncell + c);
+            dm = m;
+            dc = c;
+        }
+#pragma unroll
+        for (int s = 0; s < NS; ++s) rh[s] = drho[s];
+    }
+    template <int NS>
+    __device__ __forceinline__ float2 snap(const float2* q0, int ncell, int m, int c, int e, int s) {
+        if (m != qm || c != qc || e != qe) {
+#pragma unroll
+            for (int k = 0; k < NS; ++k) dq[k] = q0[(int64_t)k * ncell + c];
+            qm = m;
+            qc = c;
+            qe = e;
+        }
+        float2 v = dq[0];
+#pragma unroll
+        for (int k = 1; k < NS; ++k)
+            if (k == s) v = dq[k];
+        return v;
+    }
 };
 
 template <class Pol>
@@ -527,11 +568,9 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
     const int64_t base = M.cell_off;
     if (p.ir >= 0) {
         c = G::cell(M, p);
+        pol.template density<NS>(P.rho + base, M.ncell, p.m, c, rh);
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            rh[s] = __ldg(P.rho + base + (int64_t)s * M.ncell + c);
-            alpha = alpha + rh[s] * T.kext[s * nl + p.lam];
-        }
+        for (int s = 0; s < NS; ++s) alpha = alpha + rh[s] * T.kext[s * nl + p.lam];
     }
     // Safety distance: an interaction closer than the isotropic distance to the nearest
     // wall needs no wall solve (the common case in optically thick cells).
@@ -589,7 +628,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         float aR = 0.0f;
         if (cond && 0.999f * p.dmax * alpha >= P.mrw_tauthres) {
 #pragma unroll
-            for (int s = 0; s < NS; ++s) qv[s] = qa[base + (int64_t)s * M.ncell + c];
+            for (int s = 0; s < NS; ++s) qv[s] = pol.template snap<NS>(qa + base, M.ncell, p.m, c, p.epoch, s);
             if (pol.cached(p.m, c, p.epoch, 0)) {
                 aR = pol.cached_value(0);
             } else {
@@ -716,7 +755,8 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
-                p.lam = reemit_lambda(pol, T, nl, qa[idx], sp, sb.uq, sb.urow, sb.ucdf);
+                const float2 qs = pol.template snap<NS>(qa + base, M.ncell, p.m, c, p.epoch, sp);
+                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf);
                 {
                     float mu = 2.0f * ev.umu - 1.0f;
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
