@@ -56,8 +56,8 @@ def parse():
     ap.add_argument("--lnprob-walkers", type=int, default=0,
                     help="also time the batched MCMC lnprob of this many walkers (0: off)")
     ap.add_argument("--lnprob-packets", type=int, default=100000)
-    ap.add_argument("--cpu-models", type=int, default=8)
-    ap.add_argument("--cpu-packets", type=int, default=100000)
+    ap.add_argument("--cpu-models", type=int, default=64)
+    ap.add_argument("--cpu-packets", type=int, default=20000)
     ap.add_argument("--timelimit", type=float, default=1800.0,
                     help="device-side deadline per timed thermal run (s)")
     ap.add_argument("--warmup-deadline", type=float, default=10.0,
@@ -130,7 +130,8 @@ def build_models(args, rank):
 
 
 def cpu_sample(models, args, threads):
-    """The CPU restatement on the first cpu-models walkers at cpu-packets packets each, in
+    """The CPU restatement on the first cpu-models walkers (all of them by default, so the
+    sample has the workload's mix of light and heavy walkers) at cpu-packets packets each, in
     its FP64-geometry build (native double precision is the fast choice on host cores)."""
     from oracle import orc  # noqa: F401  (CPU baseline leg only)
     from tests import _cases
