@@ -45,3 +45,45 @@ def test_run_thermal_keyword_mapping():
         warnings.simplefilter("always")
         thermal._options(dict(not_a_keyword=1))
     assert any("not_a_keyword" in str(x.message) for x in w)
+
+
+def _scat_plan(L, nlam=3, nspec=1, nphot=1000, kabs=None, r=None):
+    import ctypes as C
+    import numpy as np
+    r = np.logspace(12, 15, 11) if r is None else r
+    t = np.linspace(0, np.pi / 2, 9)
+    p = np.array([0.0, 2 * np.pi])
+    rad, tem = np.array([1.4e11]), np.array([4000.0])
+    lam = np.logspace(0, 1, nlam)
+    ka = np.ones((nspec, nlam)) if kabs is None else kabs
+    ks = np.ones((nspec, nlam))
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (r, t, p, rad, tem, lam, ka, ks)]
+    dp = C.POINTER(C.c_double)
+    ptr = [a.ctypes.data_as(dp) for a in keep]
+    desc = _lib.ModelDesc(len(r) - 1, len(t) - 1, len(p) - 1, ptr[0], ptr[1], ptr[2], 1, ptr[3],
+                          ptr[4], 0)
+    opts = _lib.ScatOptions(1, nphot, 5.0, 0, 0, 0)
+    plan = C.c_void_p()
+    st = L.pdgpu_scat_plan_create(C.byref(desc), nlam, ptr[5], nspec, ptr[6], ptr[7],
+                                  C.byref(opts), C.byref(plan))
+    return st, plan
+
+
+def test_scattering_plan_validates_arguments_and_sizes_its_workspace():
+    """Host-side plan logic of the scattering Monte Carlo (no kernels launched)."""
+    import ctypes as C
+    import numpy as np
+    L = _lib.lib()
+    st, plan = _scat_plan(L)
+    assert st == 0
+    ws, nc = C.c_size_t(), C.c_int64()
+    assert L.pdgpu_scat_plan_info(plan, C.byref(ws), C.byref(nc)) == 0
+    assert nc.value == 10 * 8 * 1
+    # cell CDF (float) and path sums (int64) per wavelength and cell dominate the workspace
+    assert ws.value >= 3 * nc.value * (4 + 8)
+    L.pdgpu_scat_plan_destroy(plan)
+    assert _scat_plan(L, nlam=0)[0] == 1                                  # no wavelengths
+    assert _scat_plan(L, nphot=0)[0] == 1                                 # no packets
+    assert _scat_plan(L, kabs=-np.ones((1, 3)))[0] == 1                   # negative opacity
+    assert _scat_plan(L, nspec=5, kabs=np.ones((5, 3)))[0] == 1           # too many species
+    assert _scat_plan(L, r=np.array([1e13, 1e12, 1e14]))[0] == 1          # unsorted radii
