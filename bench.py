@@ -121,7 +121,25 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
+def max_over_ranks(v, world, device=None):
+    """The maximum of v over all ranks (every rank's timed region ends at the slowest)."""
+    if world <= 1:
+        return float(v)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_scaling_rate(world, packets_per_rank, steps, t_max_ms):
+    """Whole-job packets/s: every rank ran its own batch in the same timed region."""
+    return world * packets_per_rank * steps / (t_max_ms / 1e3)
+
+
 def build_models(args, rank):
+    """The rank's walker batch: independent walkers per rank (seed + 1000 rank), so the
+    ranks shard the ensemble with no data-path collective."""
     from pdspy_gb300 import workloads
     if args.workload == "plain":
         args.models = 1
@@ -415,17 +433,10 @@ def main():
             launch_stats.append(plan.launch_stats())
             stats.append(plan.check_status())
 
-    def max_over_ranks(v):
-        if world > 1:
-            tt = torch.tensor([v], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            return float(tt.item())
-        return v
-
-    t_max = max_over_ranks(float(np.sum(step_ms)))
-    te = max_over_ranks(float(np.sum(e2e_ms)))
-    value = world * total_packets * args.steps / (t_max / 1e3)
-    e2e = {"value": world * total_packets * args.steps / (te / 1e3), "unit": "packets/s",
+    t_max = max_over_ranks(float(np.sum(step_ms)), world, dev)
+    te = max_over_ranks(float(np.sum(e2e_ms)), world, dev)
+    value = weak_scaling_rate(world, total_packets, args.steps, t_max)
+    e2e = {"value": weak_scaling_rate(world, total_packets, args.steps, te), "unit": "packets/s",
            "h2d_bytes_per_step": int(host_rho.numel() * 4),
            "d2h_bytes_per_step": int(host_T.numel() * 8)}
 
