@@ -41,7 +41,7 @@ def _worker(rank, world, port, out):
 
 def test_two_ranks_shard_walkers_and_take_the_slowest_time():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.start_processes(_worker, args=(world, _free_port(), out), nprocs=world,
                        start_method="spawn", join=True)
     m0, t0, r0, _ = out[0]
