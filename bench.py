@@ -440,7 +440,7 @@ def main():
            "h2d_bytes_per_step": int(host_rho.numel() * 4),
            "d2h_bytes_per_step": int(host_T.numel() * 8)}
 
-    # roofline of the dominant kernel (the transport launches)
+    # roofline of the walk launches (transport and continuation kernels)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -464,7 +464,10 @@ def main():
     achieved = (alg_bytes / n_launch) / (avg_launch / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "mc_transport_kernel", "peak_source": "measured" if peaks else "fallback",
+                "kernel": "mc_transport_kernel + mc_continue_kernel (every walk launch)",
+                "peak_source": "measured" if peaks else "fallback",
+                "traffic_source": "null: ncu DRAM bytes per walk launch are 0.26-0.35 MB on the "
+                                  "plain disk (profiles/), the working set stays in L2",
                 "launches_per_step": n_launch, "kernel_ms_per_step": float(np.sum(lm)),
                 "algorithmic_bytes_per_step": int(alg_bytes)}
 
