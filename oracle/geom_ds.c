@@ -218,8 +218,11 @@ static int candidate(const Geo* G, const Pkt* p, const Frame* f, int k, float* o
 /* One Newton step on the selected wall (taken only when it is a small correction).  The
  * refined distance is a pair (s - correction): one float cannot place the packet on the
  * wall (its spacing at 1e12 cm is 1e5 cm). */
-static ds refine(const Geo* G, const Pkt* p, const Frame* f, int k, float s) {
-    ds X = ds_move(f->x, s, f->kx), Y = ds_move(f->y, s, f->ky), Z = ds_move(f->z, s, f->kz);
+/* Residual f and derivative f' of wall candidate k's equation at distance sd. */
+static void residual(const Geo* G, const Pkt* p, const Frame* f, int k, ds sd, float* fv_out,
+                     float* fd_out) {
+    const float s = sd.h;
+    ds X = ds_move2(f->x, sd, f->kx), Y = ds_move2(f->y, sd, f->ky), Z = ds_move2(f->z, sd, f->kz);
     float fv = 0.0f, fd = 0.0f;
     if (k == 0 || k == 1) {
         int i = (k == 1) ? p->ir : ((p->ir < 0) ? 0 : p->ir + 1);
@@ -247,11 +250,28 @@ static ds refine(const Geo* G, const Pkt* p, const Frame* f, int k, float s) {
         fv = ds_add(ds_mulf(X, G->sphf[k1]), ds_mulf(Y, -G->cphf[k1])).h;
         fd = f->kx * G->sphf[k1] - f->ky * G->cphf[k1];
     }
-    ds r;
+    *fv_out = fv;
+    *fd_out = fd;
+}
+
+/* Newton refinement of candidate k's single-precision root s (residual in pairs); a first
+ * correction above 1e-6 s (near-tangent crossing) is followed by a second step. */
+static ds refine(const Geo* G, const Pkt* p, const Frame* f, int k, float s) {
+    float fv, fd;
+    ds r, s0 = {s, 0.0f};
+    residual(G, p, f, k, s0, &fv, &fd);
     if (fd != 0.0f) {
         float d = fv / fd;
         if (fabsf(d) <= 1.0e-3f * s + f->tol) {
             r = ds_fast2(s, -d);
+            if (fabsf(d) > 1.0e-6f * s && r.h > 0.0f) {
+                residual(G, p, f, k, r, &fv, &fd);
+                if (fd != 0.0f) {
+                    float d2 = fv / fd;
+                    ds c = {-d2, 0.0f};
+                    if (fabsf(d2) <= fabsf(d)) r = ds_add(r, c);
+                }
+            }
             if (!(r.h > 0.0f)) { r.h = 0.0f; r.l = 0.0f; }
             return r;
         }

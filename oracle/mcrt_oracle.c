@@ -1075,6 +1075,33 @@ static double invert_temperature(const Tables* T, int s, int64_t E, double m, do
     return T->Tinv[lo] + (T->Tinv[lo + 1] - T->Tinv[lo]) * ((q - F[lo]) / (F[lo + 1] - F[lo]));
 }
 
+/* One wall solve of the walk, exposed for the geometry unit tests: the packet at pos
+ * (cm; held as a double-single pair, or as doubles when fp64 is set) moving along dir in
+ * cell (ir, itv, ip) having entered through last_wall.  Returns 0 and the exit distance and
+ * wall code, 1 on an invalid grid. */
+int orc_wall_solve(const orc_grid* grid, const double pos[3], const float dir[3], int ir,
+                   int itv, int ip, int last_wall, int fp64, double* dist, int* wall) {
+    Geo G;
+    if (orc__make_geo(grid, &G)) { orc__free_geo(&G); return 1; }
+    Pkt p;
+    memset(&p, 0, sizeof(p));
+    p.x = pos[0]; p.y = pos[1]; p.z = pos[2];
+    p.sx.h = (float)pos[0]; p.sx.l = (float)(pos[0] - (double)p.sx.h);
+    p.sy.h = (float)pos[1]; p.sy.l = (float)(pos[1] - (double)p.sy.h);
+    p.sz.h = (float)pos[2]; p.sz.l = (float)(pos[2] - (double)p.sz.h);
+    p.kx = dir[0]; p.ky = dir[1]; p.kz = dir[2];
+    p.ir = ir; p.itv = itv; p.ip = ip;
+    p.last_wall = last_wall;
+    if (fp64) {
+        *dist = orc__next_wall(&G, &p, wall);
+    } else {
+        ds d = orc__next_wall_ds(&G, &p, wall);
+        *dist = (double)d.h + (double)d.l;
+    }
+    orc__free_geo(&G);
+    return 0;
+}
+
 int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* stars,
                 const float* rho, const orc_opts* o, int64_t* energy, double* temperature,
                 int64_t* escape, int64_t* cell_crossings, orc_stats* stats) {

@@ -108,6 +108,13 @@ double orc_build_tables(const orc_dust* dust, const orc_stars* stars, double* F,
                         float* cdf, double* Finv, float* star_cdf, float* kplanck,
                         float* kross);
 
+/* One wall solve of the walk (double-single, or FP64 when fp64 != 0), for the geometry
+ * unit tests: exit distance (cm) and wall code (1 inner sphere, 2 outer sphere, 3 lower-
+ * index cone, 4 higher-index cone, 5 lower phi plane, 6 higher phi plane) of a packet at
+ * pos moving along dir in cell (ir, itv, ip), itv the virtual theta index. */
+int orc_wall_solve(const orc_grid* grid, const double pos[3], const float dir[3], int ir,
+                   int itv, int ip, int last_wall, int fp64, double* dist, int* wall);
+
 /* Thermal Monte Carlo.  energy[s][cell] receives the int64 fixed-point absorbed
  * energy (unit = packet energy / 2^20), temperature[s][cell] the dust temperature
  * in K.  escape[nlam] (optional) counts escaping packets per wavelength bin;

@@ -104,6 +104,21 @@ def cbrt01(x):
     return lib().orc_cbrt01(C.c_float(x))
 
 
+def wall_solve(r_edges, th_edges, ph_edges, pos, direction, ir, itv, ip, last_wall=0,
+               fp64=False):
+    """(distance, wall code) of one wall solve of the walk (see mcrt_oracle.h)."""
+    keep = _Keep()
+    g = _grid(r_edges, th_edges, ph_edges, keep)
+    P = (C.c_double * 3)(*[float(x) for x in pos])
+    D = (C.c_float * 3)(*[float(x) for x in direction])
+    d, w = C.c_double(), C.c_int()
+    rc = lib().orc_wall_solve(C.byref(g), P, D, int(ir), int(itv), int(ip), int(last_wall),
+                              int(bool(fp64)), C.byref(d), C.byref(w))
+    if rc:
+        raise ValueError("oracle rejected the grid")
+    return d.value, w.value
+
+
 def sincospif2(u):
     s, c = C.c_float(), C.c_float()
     lib().orc_sincospif2(C.c_float(u), C.byref(s), C.byref(c))

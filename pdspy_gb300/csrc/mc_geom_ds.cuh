@@ -232,10 +232,14 @@ __device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const Pkt
 // a small correction (a root of another branch is never jumped to).  The refined distance
 // is returned as a pair (s - correction): a single float cannot place the packet on the
 // wall (its spacing at 1e12 cm is 1e5 cm).  The result is >= 0.
-__device__ inline ds refine_ds(const McModel& M, const WallsS& W, const PktS& p,
-                               const FrameS& f, int k, float s) {
-    ds X = ds_move(f.x, s, f.kx), Y = ds_move(f.y, s, f.ky), Z = ds_move(f.z, s, f.kz);
-    float fv = 0.0f, fd = 0.0f;
+// Residual f and derivative f' of wall candidate k's equation at distance sd along the ray.
+__device__ __forceinline__ void wall_residual(const McModel& M, const WallsS& W, const PktS& p,
+                                              const FrameS& f, int k, ds sd, float& fv,
+                                              float& fd) {
+    const float s = sd.h;
+    ds X = ds_move2(f.x, sd, f.kx), Y = ds_move2(f.y, sd, f.ky), Z = ds_move2(f.z, sd, f.kz);
+    fv = 0.0f;
+    fd = 0.0f;
     if (k == 0 || k == 1) {
         int i = (k == 1) ? p.ir : ((p.ir < 0) ? 0 : p.ir + 1);
         ds r2 = ds_add(ds_add(ds_sqr(X), ds_sqr(Y)), ds_sqr(Z));
@@ -262,10 +266,26 @@ __device__ inline ds refine_ds(const McModel& M, const WallsS& W, const PktS& p,
         fv = ds_add(ds_mulf(X, W.SP[k1]), ds_mulf(Y, -W.CP[k1])).h;
         fd = f.kx * W.SP[k1] - f.ky * W.CP[k1];
     }
+}
+
+// Newton refinement of candidate k's single-precision root s, the residual evaluated in
+// pairs.  A first correction larger than 1e-6 s (a near-tangent crossing, where the
+// single-precision root is poorly conditioned) is followed by a second step.
+__device__ inline ds refine_ds(const McModel& M, const WallsS& W, const PktS& p,
+                               const FrameS& f, int k, float s) {
+    float fv, fd;
+    wall_residual(M, W, p, f, k, ds{s, 0.0f}, fv, fd);
     if (fd != 0.0f) {
         float d = fv / fd;
         if (fabsf(d) <= 1.0e-3f * s + f.tol) {
             ds r = ds_fast2(s, -d);
+            if (fabsf(d) > 1.0e-6f * s && r.h > 0.0f) {
+                wall_residual(M, W, p, f, k, r, fv, fd);
+                if (fd != 0.0f) {
+                    float d2 = fv / fd;
+                    if (fabsf(d2) <= fabsf(d)) r = ds_add(r, ds{-d2, 0.0f});
+                }
+            }
             return r.h > 0.0f ? r : ds{0.0f, 0.0f};
         }
     }
