@@ -44,8 +44,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "plain"],
-                    help="batched walkers (default) or one small disk (plain)")
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "plain", "envelope", "spiral"],
+                    help="batched walkers (default), one small disk (plain), the disk plus "
+                         "envelope on 256 x 256 cells (envelope) or four phases of the 3-D "
+                         "two-population spiral disk on 128^3 cells (spiral)")
     ap.add_argument("--models", type=int, default=64)
     ap.add_argument("--packets", type=int, default=1000000, help="packets per model")
     ap.add_argument("--seed", type=int, default=0)
@@ -144,6 +147,14 @@ def build_models(args, rank):
     if args.workload == "plain":
         args.models = 1
         return [workloads.small_disk()]
+    if args.workload == "envelope":
+        args.models = 1
+        return [workloads.disk_envelope(nr=256, ntheta=256)]
+    if args.workload == "spiral":
+        args.models = 4
+        rng = np.random.default_rng(args.seed + 1000 * rank)
+        return [workloads.spiral_disk(nr=128, ntheta=128, nphi=128, mass=1e-4,
+                                      phase=float(ph)) for ph in rng.uniform(0, 2 * np.pi, 4)]
     return workloads.walker_models(n=args.models, seed=args.seed + 1000 * rank)
 
 
@@ -341,6 +352,10 @@ def vis_rate(dev, seed):
 def workload_name(args):
     if args.workload == "plain":
         return "plain-disk-100x100-%g-packets-mrw" % args.packets
+    if args.workload == "envelope":
+        return "disk-envelope-256x256-%g-packets-mrw" % args.packets
+    if args.workload == "spiral":
+        return "spiral-3d-128^3-two-populations-4-phases-%g-packets-each-mrw" % args.packets
     return "batched-%d-walker-disks-%g-packets-each-mrw" % (args.models, args.packets)
 
 
