@@ -241,6 +241,12 @@ pdgpu_status pdgpu_image_plan_upload(pdgpu_image_plan* plan, void* workspace, si
  * at 1 pc (the unit of radmc3d/read.pyx:25-152 before pdspy's Jy conversion). */
 pdgpu_status pdgpu_image_run(pdgpu_image_plan* plan, const float* alpha, const float* S,
                              double* image, void* workspace, size_t bytes, void* stream);
+/* Whole-field flux of an image from pdgpu_image_run: flux[l] (device double [nlam],
+ * erg/s/cm^2/Hz at 1 pc) = pixel solid angle at 1 pc x sum of the pixels of plane l -- the
+ * spectrum "radmc3d spectrum" writes (pdspy/radmc3d/run.py:69-155, read.pyx:337-375),
+ * which run_sed scales by 1/dpc^2 and converts to Jy (pdspy/modeling/Model.py:639-648). */
+pdgpu_status pdgpu_image_flux(pdgpu_image_plan* plan, const double* image, double* flux,
+                              void* stream);
 /* Reverse-mode derivative of pdgpu_image_run: given dL/dimage (device double, as image)
  * writes dL/dalpha and dL/dS (device double [nlam][ncell]).  No counterpart in the
  * reference, which fits models by sampling (pdspy/utils/emcee.py:6-61). */

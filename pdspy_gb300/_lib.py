@@ -88,7 +88,7 @@ EXPORTS = [
     "pdgpu_mctherm", "pdgpu_mctherm_workspace_bytes", "pdgpu_mc_plan_launch_ms",
     "pdgpu_mc_plan_set_deadline",
     "pdgpu_image_plan_create", "pdgpu_image_plan_destroy", "pdgpu_image_plan_info",
-    "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint",
+    "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint", "pdgpu_image_flux",
     "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint", "pdgpu_mctherm_static",
     "pdgpu_scat_plan_create", "pdgpu_scat_plan_destroy", "pdgpu_scat_plan_info",
     "pdgpu_scat_plan_upload", "pdgpu_scat_run", "pdgpu_scat_plan_stats",
@@ -152,6 +152,8 @@ def lib(build_if_missing=True):
     L.pdgpu_image_plan_upload.argtypes = [vp, vp, sz, vp]
     L.pdgpu_image_run.restype = i32
     L.pdgpu_image_run.argtypes = [vp, vp, vp, vp, vp, sz, vp]
+    L.pdgpu_image_flux.restype = i32
+    L.pdgpu_image_flux.argtypes = [vp, vp, vp, vp]
     L.pdgpu_image_adjoint.restype = i32
     L.pdgpu_image_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp]
     L.pdgpu_mctherm_static.restype = i32

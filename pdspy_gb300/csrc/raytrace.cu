@@ -201,6 +201,24 @@ __global__ void rt_reduce_kernel(const int64_t* off, const float* ray_I, int npi
 }
 
 // Point stars at the origin: optical depth to the observer, flux into the centre pixel.
+// Flux of every wavelength plane: flux[l] = omega * sum_pix image[l][pix], one block per
+// wavelength, fixed-order tree sum (deterministic).
+__global__ void __launch_bounds__(256) rt_flux_kernel(const double* image, int npix, double omega,
+                                                      double* flux) {
+    __shared__ double s[256];
+    const int l = blockIdx.x;
+    const double* im = image + (size_t)l * npix;
+    double a = 0.0;
+    for (int i = threadIdx.x; i < npix; i += blockDim.x) a += im[i];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) flux[l] = s[0] * omega;
+}
+
 __global__ void rt_star_kernel(RtParams P, const double* star_flux, double omega, double* image,
                                int adjoint) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -466,6 +484,13 @@ static RtParams rt_params(pdgpu_image_plan* P, char* w, const float* alpha, cons
 static int rt_grid(pdgpu_image_plan* P) {
     int64_t want = (P->nrays + 127) / 128;
     return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)P->nsm * 16));
+}
+
+pdgpu_status pdgpu_image_flux(pdgpu_image_plan* P, const double* image, double* flux,
+                              void* stream) {
+    if (!P || !image || !flux) return PDGPU_INVALID_ARG;
+    rt_flux_kernel<<<P->nlam, 256, 0, (cudaStream_t)stream>>>(image, P->npix, P->omega, flux);
+    return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_CUDA_ERROR;
 }
 
 pdgpu_status pdgpu_image_run(pdgpu_image_plan* P, const float* alpha, const float* S,

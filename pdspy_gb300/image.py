@@ -189,6 +189,15 @@ class ImagePlan:
                    "pdgpu_image_run")
         return out
 
+    def flux(self, image_1pc):
+        """Whole-field flux per wavelength at 1 pc (erg/s/cm^2/Hz), float64 [nlam]."""
+        img = image_1pc.to(torch.float64).contiguous()
+        out = torch.empty(self.nlam, dtype=torch.float64, device=self.device)
+        _lib.check(self.L.pdgpu_image_flux(self._plan, img.data_ptr(), out.data_ptr(),
+                                           torch.cuda.current_stream(self.device).cuda_stream),
+                   "pdgpu_image_flux")
+        return out
+
     def adjoint(self, alpha, S, grad_image):
         """(dL/dalpha, dL/dS) float64 [nlam, ncell] for dL/dimage."""
         self._check_inputs(alpha, S)
@@ -295,8 +304,7 @@ def run_sed(model, name=None, nphot=1e6, incl=0, pa=0, phi=0, dpc=1, loadlambda=
                      max_refine=max_refine, refine_factor=refine_factor, device=dev)
     alpha, S = model_sources(model, lam_um, dev, nphot_scat=int(nphot), **_scat_keywords(keywords))
     inten = plan.run(alpha, S)
-    omega = (pixel_cm / pc) ** 2
-    flux_1pc = (inten.sum(dim=(1, 2)) * omega).cpu().numpy()   # erg/s/cm^2/Hz at 1 pc
+    flux_1pc = plan.flux(inten).cpu().numpy()                 # erg/s/cm^2/Hz at 1 pc
     flux = flux_1pc / Jy * (1.0 / dpc) ** 2
     model.spectra[name] = Spectrum(wave=lam_um, flux=flux)
     return model.spectra[name]

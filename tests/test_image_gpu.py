@@ -97,3 +97,17 @@ def test_sed_optically_thin_matches_volume_emission(cuda):
     d = 140 * K.pc
     expect = L / (4 * np.pi * d ** 2) / K.Jy + image.star_flux_1pc(g, lam) / 140 ** 2 / K.Jy
     assert np.allclose(sed.flux, expect, rtol=0.02), sed.flux / expect
+
+
+def test_image_flux_is_omega_times_pixel_sum(cuda):
+    m = _cases.image_model("disk", nr=12, ntheta=12)
+    lam = np.array([1300.0, 100.0, 10.0])
+    r, _, _ = thermal.grid_arrays(m.grid)
+    npix = 40
+    pixel_cm = 2.02 * r[-1] / npix
+    plan = image.ImagePlan(m.grid, npix, pixel_cm, lam, incl=35.0, device=cuda)
+    a, s = image.model_sources(m, lam, cuda)
+    img = plan.run(a, s)
+    got = plan.flux(img).cpu().numpy()
+    expect = img.sum(dim=(1, 2)).cpu().numpy() * (pixel_cm / K.pc) ** 2
+    assert np.allclose(got, expect, rtol=1e-12, atol=0)
