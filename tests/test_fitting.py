@@ -37,3 +37,20 @@ def test_build_model_grid_and_densities():
     assert np.isclose(g.w1[-1], p["R_env"]) and np.isclose(g.w2[-1], np.pi / 2)
     assert len(g.density) == 2 and g.density[0].shape == (99, 100, 1)
     assert np.all(g.density[1] >= 0) and g.density[1].max() > 0
+
+
+def test_lnlike_visibility_term_as_pdspy_writes_it():
+    """utils/emcee.py:31-43: -0.5 sum (Re_d - Re_m)^2 w - sum log(w_good / 2 pi), the same
+    for Im, zero-weight points excluded from the log terms."""
+    from pdspy_gb300 import vis
+    rng = np.random.default_rng(4)
+    n = 50
+    w = rng.uniform(1.0, 5.0, n)
+    w[:5] = 0.0
+    d = vis.UVData(rng.normal(size=n), rng.normal(size=n), rng.normal(size=n),
+                   rng.normal(size=n), w)
+    re, im = rng.normal(size=n), rng.normal(size=n)
+    good = w > 0
+    expect = (-0.5 * np.sum((d.real - re) ** 2 * w) - np.sum(np.log(w[good] / (2 * np.pi))) +
+              -0.5 * np.sum((d.imag - im) ** 2 * w) - np.sum(np.log(w[good] / (2 * np.pi))))
+    assert fitting._lnlike_vis(re, im, d) == expect

@@ -28,14 +28,14 @@ def planck(nu, T):
     return 2 * h * nu ** 3 / c ** 2 / np.expm1(h * nu / (k * T))
 
 
-def _shell_grid(nr=20, nt=10, rin=1.0, rout=100.0):
+def _shell_grid(nr=20, nt=10, rin=1.0, rout=100.0, nphi=1, mirror=True):
     r = np.logspace(np.log10(rin), np.log10(rout), nr + 1) * AU
-    th = np.linspace(0.0, np.pi / 2, nt + 1)
-    ph = np.array([0.0, 2.0 * np.pi])
+    th = np.linspace(0.0, np.pi / 2 if mirror else np.pi, nt + 1)
+    ph = np.linspace(0.0, 2.0 * np.pi, nphi + 1)
     Vr = (r[1:] ** 3 - r[:-1] ** 3) / 3.0
-    Vt = 2.0 * (np.cos(th[:-1]) - np.cos(th[1:]))
-    V = Vr[:, None] * Vt[None, :] * 2.0 * np.pi
-    return r, th, ph, V
+    Vt = (2.0 if mirror else 1.0) * (np.cos(th[:-1]) - np.cos(th[1:]))
+    V = Vr[:, None, None] * Vt[None, :, None] * np.diff(ph)[None, None, :]
+    return r, th, ph, V.reshape(nr, -1)
 
 
 def _lstar(lam):
@@ -62,8 +62,9 @@ def test_math_helpers_accuracy():
     assert np.max(np.abs(c / np.cbrt(xs.astype(np.float64)) - 1)) < 3e-7
 
 
-def test_thin_shell_point_source():
-    r, th, ph, V = _shell_grid()
+@pytest.mark.parametrize("nphi,mirror", [(1, True), (6, False)])
+def test_thin_shell_point_source(nphi, mirror):
+    r, th, ph, V = _shell_grid(nphi=nphi, mirror=mirror)
     lam = np.array([1.0, 3.0])
     ncell = V.size
     o = orc.mcscat(r, th, ph, np.full((1, ncell), 1e-25), lam, np.zeros((1, 2)),
