@@ -12,11 +12,18 @@ A step is one full thermal run of the batch (all epochs, both continuation stage
 temperature inversion).  ``value`` is packets/s with the densities resident in HBM (CUDA
 events around the run); ``e2e`` is the same step through the public API with host arrays,
 timed on the same stream from the pinned H2D copy of the densities to the D2H copy of the
-temperatures.  The longest packet walk of this workload (about 1e8 interactions for one
-walker at 1e6 packets) sets most of a step's time, so the default is one timed step and
-warm-up runs are cut at a short device deadline.  The reference arm (``--impl reference``)
-times the CPU restatement of the same algorithm (the reference's own path is the external
-RADMC-3D binary, which is not available) on a bounded sample of the workload.
+temperatures.  The longest packet walk of this workload (3e7 interactions for one walker
+at 1e6 packets with the default seed; the walk lengths are heavy-tailed) sets most of a
+step's time, so the default is one timed step and warm-up runs are cut at a short device
+deadline.  The reference arm (``--impl reference``) times the CPU restatement of the same
+algorithm (the reference's own path is the external RADMC-3D binary, which is not
+available) on a bounded sample of the workload: every walker at 2e4 packets.
+
+The same JSON line carries the adjoint gradient rate, the scattering source of an SED
+(with its CPU restatement), gridded vs direct visibility sampling and, with
+``--lnprob-walkers``, the batched MCMC lnprob; ``--workload plain|envelope|spiral`` runs
+the single small disk, the disk plus envelope (256 x 256 cells) or four phases of the 3-D
+spiral (128^3 cells) instead of the walkers.
 
 With torchrun (N > 1) every rank runs its own independent batch of walkers (the models
 shard with no data-path collective): weak scaling, value = all ranks' packets / max time.
