@@ -23,7 +23,9 @@ over an MPI pool).  ``lnprob_batched`` evaluates a whole ensemble in one go:
 Scope: the "truncated" power-law disk with an optional "ulrich-extended" envelope (its
 centrifugal radius = R_disk, as YSOModel does unless rcent_ne_rdisk), the visibility
 likelihood (lnlike's image and SED terms need data products outside this path), and one
-dust model for disk and envelope (pdspy's DustGenerator tables are not available).
+dust model for disk and envelope (pdspy's DustGenerator tables are not available).  The
+free-free point source run_disk_model adds to the visibilities (:325-334; F_nu_ff
+defaults to 1e-20 Jy) is not added.
 """
 import subprocess
 
