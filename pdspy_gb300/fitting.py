@@ -24,8 +24,9 @@ Scope: the "truncated" power-law disk with an optional "ulrich-extended" envelop
 centrifugal radius = R_disk, as YSOModel does unless rcent_ne_rdisk), the visibility
 likelihood (lnlike's image and SED terms need data products outside this path), and one
 dust model for disk and envelope (pdspy's DustGenerator tables are not available).  The
-free-free point source run_disk_model adds to the visibilities (:325-334; F_nu_ff
-defaults to 1e-20 Jy) is not added.
+free-free point source run_disk_model adds to the real part of the visibilities
+(:325-334, pdspy/spectroscopy/freefree.py, interferometry/model.py:102-104) is added the
+same way.
 """
 import subprocess
 
@@ -56,6 +57,7 @@ def base_parameters():
         "i": e(45., 0., 180.), "pa": e(0., 0., 360.), "x0": e(0., -0.1, 0.1),
         "y0": e(0., -0.1, 0.1), "dpc": e(140., 1., 1e6, prior="box", sigma=0.),
         "flux_unc1": e(1., 0.5, 1.5, prior="box", sigma=0.),
+        "logF_nu_ff": e(-20., -30., 0.), "lognu_turn": e(0., -1., 2.), "pl_turn": e(0.6, 0., 2.),
     }
 
 
@@ -140,6 +142,25 @@ def build_model(p, dust, lam_um, device):
     return m
 
 
+def freefree(nu, F_nu_ff, nu_turn, pl_turn):
+    """pdspy's free-free spectrum (pdspy/spectroscopy/freefree.py:3-17), Jy."""
+    nu = np.asarray(nu, dtype=np.float64)
+    flux = np.where(nu < nu_turn, F_nu_ff * (nu / nu_turn) ** pl_turn,
+                    F_nu_ff * (nu / nu_turn) ** -0.1)
+    return np.where(nu > 1.0e13, 0.0, flux)
+
+
+def freefree_real(u, v, freq, p):
+    """Real part of the free-free point source at (x0, y0) run_disk_model adds to the model
+    visibilities (run_disk_model.py:325-334; point_model, interferometry/model.py:102-104,
+    with its 3.14159)."""
+    f = float(freefree(np.mean(freq), p.get("F_nu_ff", 0.0), p.get("nu_turn", 1.0) * 1e9,
+                       p.get("pl_turn", 0.6)))
+    x0 = float(p.get("x0", 0.0)) * arcsec
+    y0 = float(p.get("y0", 0.0)) * arcsec
+    return f * np.cos(2 * 3.14159 * (np.asarray(u) * x0 + np.asarray(v) * y0))
+
+
 def _lnlike_vis(re, im, data):
     """lnlike's visibility term (utils/emcee.py:31-43), numerically as pdspy writes it."""
     w = data.weights
@@ -166,7 +187,8 @@ def model_visibilities(m, p, vis_set, device, pad=2, nphot_image=1e5):
     u = torch.as_tensor(data.u, dtype=torch.float32, device=device)
     v = torch.as_tensor(data.v, dtype=torch.float32, device=device)
     re, im = vis.VisFFT.apply(plane, u, v, geo, pad)
-    return re.cpu().numpy(), im.cpu().numpy()
+    re = re.cpu().numpy() + freefree_real(data.u, data.v, data.freq, p)
+    return re, im.cpu().numpy()
 
 
 def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=None,

@@ -54,3 +54,19 @@ def test_lnlike_visibility_term_as_pdspy_writes_it():
     expect = (-0.5 * np.sum((d.real - re) ** 2 * w) - np.sum(np.log(w[good] / (2 * np.pi))) +
               -0.5 * np.sum((d.imag - im) ** 2 * w) - np.sum(np.log(w[good] / (2 * np.pi))))
     assert fitting._lnlike_vis(re, im, d) == expect
+
+
+def test_freefree_matches_pdspy_formula():
+    """pdspy/spectroscopy/freefree.py:3-17 and the point source of
+    interferometry/model.py:102-104 (real part)."""
+    nu = np.array([1e8, 1e9, 3e10, 2e13])
+    F, nt, pl = 1e-3, 5e9, 0.6
+    expect = np.where(nu < nt, F * (nu / nt) ** pl, F * (nu / nt) ** -0.1)
+    expect = np.where(nu > 1e13, 0.0, expect)
+    assert np.array_equal(fitting.freefree(nu, F, nt, pl), expect)
+    p = {"F_nu_ff": F, "nu_turn": 5.0, "pl_turn": pl, "x0": 0.02, "y0": -0.01}
+    u, v = np.array([1e5, -3e5]), np.array([2e5, 4e4])
+    from pdspy_gb300.constants import arcsec
+    ff = fitting.freefree(2.3e11, F, 5e9, pl)
+    pt = ff * np.exp(-2 * 3.14159 * (0 + 1j * (u * 0.02 * arcsec + v * -0.01 * arcsec)))
+    assert np.allclose(fitting.freefree_real(u, v, [2.3e11], p), pt.real, rtol=1e-14)
