@@ -378,9 +378,10 @@ def run_reference(args, world, rank):
         v, dt = cpu_sample(models, args, threads)
         vals.append(v)
         times.append(dt)
-    value = float(np.sum([args.cpu_models * args.cpu_packets] * args.steps) / np.sum(times))
-    sample = "%d walkers x %d packets (of the %d x %g workload), CPU restatement (FP64 geometry), %d threads" % (
-        args.cpu_models, args.cpu_packets, args.models, args.packets, threads)
+    nm = min(args.cpu_models, len(models))
+    value = float(nm * args.cpu_packets * args.steps / np.sum(times))
+    sample = "%d models x %d packets (of the %d x %g workload), CPU restatement (FP64 geometry), %d threads" % (
+        nm, args.cpu_packets, args.models, args.packets, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "packets/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(times) * 1e3), "higher_is_better": True,
@@ -513,8 +514,8 @@ def main():
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_sample(models, args, os.cpu_count())
         cpu = {"value": v, "unit": "packets/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "%d walkers x %d packets of the workload, CPU restatement (%.1f s)" %
-               (args.cpu_models, args.cpu_packets, dt)}
+               "sample": "%d models x %d packets of the workload, CPU restatement (%.1f s)" %
+               (min(args.cpu_models, len(models)), args.cpu_packets, dt)}
 
     K, P = plan.opts.nepoch, plan.opts.npilot
     # start + (prep + transport) per pass and epoch + two continuation launches +
