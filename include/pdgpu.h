@@ -15,8 +15,16 @@
  *                       radmc3d.read.image (radmc3d/read.pyx:25-152).
  *   pdgpu_image_adjoint reverse-mode derivative of the same ray trace; no counterpart in
  *                       the reference (pdspy fits by sampling, utils/emcee.py:6-61).
- *   pdgpu_vis_*         direct Fourier transform of an image at uv points and the chi^2
- *                       of interferometry/libinterferometry.pyx:610-633 (chisq_calc).
+ *   pdgpu_image_flux    the whole-field spectrum of radmc3d.run.sed / read.spectrum
+ *                       behind Model.run_sed (Model.py:608-650, radmc3d/run.py:69-155).
+ *   pdgpu_vis_*         visibilities of an image at uv points: the direct sum and the
+ *                       gridded (FFT + bilinear) sampling of galario's sampleImage that
+ *                       interferometry/interpolate_model.py:11-57 calls, for the chi^2 of
+ *                       interferometry/libinterferometry.pyx:610-633 (chisq_calc).
+ *   pdgpu_scat_*        the scattering Monte Carlo RADMC-3D runs inside "radmc3d image" /
+ *                       "radmc3d spectrum" and as "radmc3d mcscat" (Model.py:258-322,
+ *                       radmc3d/run.py:40-67; nphot_scat, mc_scat_maxtauabs from
+ *                       radmc3d/write.py:33-38, :141-142).
  *
  * Conventions.  Arrays marked "device" are caller-owned device buffers; arrays marked
  * "host" are read during the call only.  Cell arrays use numpy's C order of pdspy's
@@ -164,7 +172,6 @@ pdgpu_status pdgpu_mc_plan_upload(pdgpu_mc_plan* plan, void* workspace, size_t b
 pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* plan, const float* rho, double* temperature,
                                void* workspace, size_t bytes, void* stream);
 
-/* Synchronise the stream and read the run's counters and device status. */
 /* Durations (ms, CUDA events on the run's stream) of the transport launches of the last
  * run when options.time_launches was set; returns the number written (<= capacity). */
 int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* plan, float* ms, int32_t capacity);
@@ -173,6 +180,8 @@ int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* plan, float* ms, int32_t capacity
  * radmc3d.run.thermal (radmc3d/run.py:9-38) per run instead of per plan. */
 pdgpu_status pdgpu_mc_plan_set_deadline(pdgpu_mc_plan* plan, int64_t deadline_ns);
 
+/* Synchronise the stream and read the run's counters and device status (the status a
+ * radmc3d.run.thermal subprocess reports through its exit and timeout). */
 pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* plan, const void* workspace, void* stream,
                                  pdgpu_mc_stats* stats);
 
