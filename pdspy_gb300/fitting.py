@@ -172,13 +172,15 @@ def _lnlike_vis(re, im, data):
 
 def model_visibilities(m, p, vis_set, device, pad=2, nphot_image=1e5):
     """Model visibilities (re, im) of walker m for one visibility set: run_image at the
-    set's wavelength (npix, pixelsize, incl i, pa, dpc), times flux_unc, sampled with the
-    (x0, y0) offset."""
+    set's wavelength with run_disk_model's settings (npix, pixelsize, incl i, pa, dpc,
+    1e5 scattering packets, mc_scat_maxtauabs 5; run_disk_model.py:299-306), times flux_unc,
+    sampled with the (x0, y0) offset.  One frequency channel per set (continuum data)."""
     data = vis_set["data"]
     lam_um = C_LIGHT / np.atleast_1d(data.freq)[0] / 1.0e-4
     npix, pixelsize = int(vis_set["npix"]), float(vis_set["pixelsize"])
     img = image.run_image(m, name="vis", nphot=nphot_image, npix=npix, pixelsize=pixelsize,
-                          lam=[lam_um], incl=p["i"], pa=p["pa"], dpc=p["dpc"])
+                          lam=[lam_um], incl=p["i"], pa=p["pa"], dpc=p["dpc"],
+                          mc_scat_maxtauabs=5)
     scale = float(p.get("flux_unc%d" % vis_set["index"], 1.0))
     plane = torch.as_tensor(img.image[:, :, 0, 0] * scale, dtype=torch.float32, device=device)
     geo = vis.pixel_grid(npix, pixelsize)
