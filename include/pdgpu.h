@@ -180,6 +180,21 @@ int32_t pdgpu_mc_plan_launch_ms(pdgpu_mc_plan* plan, float* ms, int32_t capacity
  * radmc3d.run.thermal (radmc3d/run.py:9-38) per run instead of per plan. */
 pdgpu_status pdgpu_mc_plan_set_deadline(pdgpu_mc_plan* plan, int64_t deadline_ns);
 
+/* Per-model time limits of a batched plan (one MCMC walker per model).  Replaces
+ * run.thermal's timelimit (radmc3d/run.py:9-38) as run_disk_model.py:251-273 applies it: each
+ * walker's own radmc3d subprocess may time out, and that walker alone scores -inf
+ * (utils/emcee.py:22-23).  deadline_ns[m] (device clock, from the start of each run; 0 = none)
+ * stops model m when it has not finished in time: its status becomes PDGPU_TIMEOUT, its
+ * remaining packets are dropped (its temperatures are then meaningless) and the other models
+ * finish with results identical to a run without the limit.  NULL clears every limit.  The
+ * plan must be uploaded; the limits stay until changed and the call waits for the stream. */
+pdgpu_status pdgpu_mc_plan_set_model_deadlines(pdgpu_mc_plan* plan, const int64_t* deadline_ns,
+                                               void* stream);
+/* Status of every model after the last run (host int32 [nmodels]: PDGPU_OK or
+ * PDGPU_TIMEOUT); waits for the stream. */
+pdgpu_status pdgpu_mc_plan_model_status(pdgpu_mc_plan* plan, const void* workspace, void* stream,
+                                        int32_t* status);
+
 /* Synchronise the stream and read the run's counters and device status (the status a
  * radmc3d.run.thermal subprocess reports through its exit and timeout). */
 pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* plan, const void* workspace, void* stream,
@@ -201,9 +216,12 @@ size_t pdgpu_mctherm_workspace_bytes(int32_t nmodels, const pdgpu_model_desc* mo
  * the workspace is a file-scope device array of PDGPU_STATIC_WORKSPACE_BYTES held by every
  * GPU that loads the library until the process exits; the caller still passes rho and
  * temperature.  The entry point calls no cudaMalloc/cudaFree.  Its first call on a device
- * looks up the array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  Runs whose workspace would exceed the array return
- * PDGPU_TOO_LARGE without touching the GPU.  All calls share the array (each run clears
+ * looks up the array's device address (cudaGetSymbolAddress) and keeps it for the life of
+ * the process, so make that first call before any stream capture, and do not keep using
+ * the library across a device reset (cudaDeviceReset) by another part of the process.
+ * Every call copies its tables in and its statistics out and waits for the stream to
+ * finish before it returns.  Runs whose workspace would exceed the array return
+ * PDGPU_TOO_LARGE before any copy or launch.  All calls share the array (each run clears
  * what it accumulates), so calls that overlap on the GPU — on different streams or host
  * threads — race; serialise them. */
 #define PDGPU_STATIC_WORKSPACE_BYTES (32u << 20)

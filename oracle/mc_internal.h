@@ -42,6 +42,9 @@ typedef struct {
     uint32_t key[2];
     uint32_t buf[4];
     uint32_t draw;
+    int64_t own_sc[4];  /* own deposits: (species, cell) keys, round-robin cache */
+    int64_t own_u[4];   /* units this packet deposited there                   */
+    int own_next;
 } Pkt;
 
 enum { W_NONE = 0, W_RIN = 1, W_ROUT = 2, W_TLO = 3, W_THI = 4, W_PLO = 5, W_PHI = 6 };

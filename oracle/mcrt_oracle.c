@@ -644,6 +644,7 @@ typedef struct {
     const Tables* T;
     const float* rho;       /* [nspec][ncell]   */
     const double* mass;     /* [nspec][ncell]   */
+    const float* wq;        /* [nspec][ncell] q per deposit unit: (float)(q_unit / mass) */
     float* qlo; float* qspan;
     int64_t* E;             /* deposits of a packet's first late_after events   */
     int64_t* Elate;         /* deposits of its later events                      */
@@ -660,13 +661,33 @@ typedef struct {
 
 static void atomic_add64(int64_t* a, int64_t v) { __atomic_fetch_add(a, v, __ATOMIC_RELAXED); }
 
+/* The packet's own deposits per (species, cell) in a four-entry round-robin cache: the
+ * reemission temperature and the MRW mean opacities of a cell are taken at the epoch's
+ * snapshot plus the packet's own deposits there (sequential B&W lets a packet trapped in
+ * an optically thick cell heat the cell it reemits from; the snapshot cannot see deposits
+ * made after it was taken). */
+#define OWNK 4
+static void own_add(Pkt* p, int64_t sc, int64_t units) {
+    for (int i = 0; i < OWNK; ++i)
+        if (p->own_sc[i] == sc) { p->own_u[i] += units; return; }
+    p->own_sc[p->own_next] = sc;
+    p->own_u[p->own_next] = units;
+    p->own_next = (p->own_next + 1) % OWNK;
+}
+
+static float own_q(const Ctx* X, const Pkt* p, int64_t sc) {
+    for (int i = 0; i < OWNK; ++i)
+        if (p->own_sc[i] == sc) return (float)p->own_u[i] * X->wq[sc];
+    return 0.0f;
+}
+
 /* Deposit target of the current event: the first late_after events of a packet feed
  * the main accumulator (read by later epochs), the rest the late accumulator. */
 #define DEP(X, p) (((X)->late_after > 0 && (p).nevents > (X)->late_after) ? (X)->Elate : (X)->E)
 
 /* Reemission wavelength for species s in cell c. */
 /* Reemission wavelength bin of species s in cell c from the uniforms (uq, urow, ucdf). */
-static int reemit_lambda(const Ctx* X, int s, int c, float uq, float urow, float ucdf) {
+static int reemit_lambda(const Ctx* X, const Pkt* p, int s, int c, float uq, float urow, float ucdf) {
     const Tables* T = X->T;
     size_t sc = (size_t)s * X->G->ncell + c;
     float q;
@@ -675,6 +696,7 @@ static int reemit_lambda(const Ctx* X, int s, int c, float uq, float urow, float
         q = (X->mass[sc] > 0.0) ? (float)((double)e * X->q_unit / X->mass[sc]) : 0.0f;
     } else {
         q = X->qlo[sc] + uq * X->qspan[sc];
+        if (X->o->own_heating) q = q + own_q(X, p, (int64_t)sc);
     }
     int j;
     float w;
@@ -684,7 +706,7 @@ static int reemit_lambda(const Ctx* X, int s, int c, float uq, float urow, float
 }
 
 /* Frozen-row interpolation of a [NROW] table at the cell's mid-epoch energy. */
-static float row_interp(const Ctx* X, const float* tab_s, int s, int c) {
+static float row_interp(const Ctx* X, const Pkt* p, const float* tab_s, int s, int c) {
     size_t sc = (size_t)s * X->G->ncell + c;
     float q;
     if (X->sequential) {
@@ -692,6 +714,7 @@ static float row_interp(const Ctx* X, const float* tab_s, int s, int c) {
         q = (X->mass[sc] > 0.0) ? (float)((double)e * X->q_unit / X->mass[sc]) : 0.0f;
     } else {
         q = X->qlo[sc] + 0.5f * X->qspan[sc];
+        if (X->o->own_heating) q = q + own_q(X, p, (int64_t)sc);
     }
     int j;
     float w;
@@ -755,6 +778,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
     const int f64 = o->fp64_walls;
     Pkt p;
     memset(&p, 0, sizeof(p));
+    for (int i = 0; i < 4; ++i) p.own_sc[i] = -1;
     p.ctr[1] = pid; p.ctr[2] = (uint32_t)o->model_id; p.ctr[3] = tag;
     p.key[0] = (uint32_t)(o->seed & 0xffffffffu);
     p.key[1] = (uint32_t)(o->seed >> 32);
@@ -853,7 +877,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
             if (cond && 0.999f * p.dmax * alpha >= o->mrw_tauthres) {
                 for (int s = 0; s < ns; ++s)
                     aR = aR + X->rho[(size_t)s * G->ncell + c] *
-                                  row_interp(X, T->kR + (size_t)s * ORC_NROW, s, c);
+                                  row_interp(X, &p, T->kR + (size_t)s * ORC_NROW, s, c);
                 tried = 0.999f * p.dmax * aR >= o->mrw_gamma;
             }
             if (tried) {
@@ -876,12 +900,15 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                     float aP = 0.0f;
                     for (int s = 0; s < ns; ++s) {
                         kp[s] = X->rho[(size_t)s * G->ncell + c] *
-                                row_interp(X, T->kP + (size_t)s * ORC_NROW, s, c);
+                                row_interp(X, &p, T->kP + (size_t)s * ORC_NROW, s, c);
                         aP = aP + kp[s];
                         float units_f = kp[s] * ell * 1048576.0f + 0.5f;
                         if (units_f > 9.0e18f) units_f = 9.0e18f;
                         int64_t units = (int64_t)units_f;
-                        if (units > 0) atomic_add64(&DEP(X, p)[(size_t)s * G->ncell + c], units);
+                        if (units > 0) {
+                            atomic_add64(&DEP(X, p)[(size_t)s * G->ncell + c], units);
+                            own_add(&p, (int64_t)s * G->ncell + c, units);
+                        }
                     }
                     /* jump to the sphere surface */
                     float dx, dy, dz;
@@ -918,7 +945,7 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                             if (us < acc) { sp = s; break; }
                         }
                     }
-                    p.lam = reemit_lambda(X, sp, c, sb[0], sb[1], sb[2]);
+                    p.lam = reemit_lambda(X, &p, sp, c, sb[0], sb[1], sb[2]);
                     p.tau = -orc_logf(ev[1]);
                     p.cell_events = 0;
                     cnt->mrw += 1;
@@ -974,7 +1001,8 @@ static int64_t run_packet(const Ctx* X, uint32_t pid, uint32_t tag, Cnt* cnt) {
                         }
                     }
                     atomic_add64(&DEP(X, p)[(size_t)sp * G->ncell + c], (int64_t)1 << ORC_EUNIT_SHIFT);
-                    p.lam = reemit_lambda(X, sp, c, sb[0], sb[1], sb[2]);
+                    own_add(&p, (int64_t)sp * G->ncell + c, (int64_t)1 << ORC_EUNIT_SHIFT);
+                    p.lam = reemit_lambda(X, &p, sp, c, sb[0], sb[1], sb[2]);
                     iso_dir(&p, ev[2], ev[3]);
                     cnt->absorptions += 1;
                 }
@@ -1061,6 +1089,10 @@ static void run_range(const Ctx* X, int64_t b0, int64_t b1, uint32_t tag, Cnt* t
     tot->mrw += mrw;
 }
 
+static double q_unit_of(const Tables* T, const orc_opts* o) {
+    return T->lum / (double)o->nphot / (double)((int64_t)1 << ORC_EUNIT_SHIFT);
+}
+
 static double invert_temperature(const Tables* T, int s, int64_t E, double m, double q_unit) {
     if (E <= 0 || !(m > 0.0)) return 0.0;
     const double* F = T->Finv + (size_t)s * ORC_NINV;
@@ -1123,6 +1155,8 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
                     double V = G.Vr[i] * G.Vt[j] * G.Vp[k];
                     mass[(size_t)s * nc + cc] = (double)rho[(size_t)s * nc + cc] * V;
                 }
+    float* wq = malloc(sizeof(float) * n);
+    for (size_t i = 0; i < n; ++i) wq[i] = (mass[i] > 0.0) ? (float)(q_unit_of(&T, o) / mass[i]) : 0.0f;
     float* qlo = calloc(n, sizeof(float));
     float* qspan = calloc(n, sizeof(float));
     int64_t* D = calloc(n, sizeof(int64_t));
@@ -1134,7 +1168,7 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
     double eps = T.lum / (double)o->nphot;
     double q_unit = eps / (double)((int64_t)1 << ORC_EUNIT_SHIFT);
     Ctx X;
-    X.G = &G; X.T = &T; X.rho = rho; X.mass = mass; X.qlo = qlo; X.qspan = qspan;
+    X.G = &G; X.T = &T; X.rho = rho; X.mass = mass; X.wq = wq; X.qlo = qlo; X.qspan = qspan;
     X.E = energy; X.escape = escape; X.ccross = cell_crossings; X.q_unit = q_unit;
     X.Elate = Elate; X.late_after = o->sequential ? 0 : o->late_after; X.pilot = 0;
     X.sequential = o->sequential; X.o = o;
@@ -1206,7 +1240,7 @@ int orc_mctherm(const orc_grid* grid, const orc_dust* dust, const orc_stars* sta
         stats->max_packet_events = maxev;
         for (int b = 0; b < 10; ++b) stats->events_hist[b] = hist[b];
     }
-    free(mass); free(qlo); free(qspan); free(D); free(Elate);
+    free(mass); free(wq); free(qlo); free(qspan); free(D); free(Elate);
     free_tables(&T);
     orc__free_geo(&G);
     return 0;

@@ -85,6 +85,9 @@ typedef struct {
                                   /* every event (0 = never)                      */
     int fp64_walls;               /* 1: FP64 positions and walls; 0: double-single */
                                   /* (pairs of floats, the GPU's default)         */
+    int own_heating;              /* 1: reemission and MRW mean opacities add the */
+                                  /* packet's own deposits in the cell (the GPU's */
+                                  /* algorithm); 0: the epoch snapshot alone      */
 } orc_opts;
 
 typedef struct {

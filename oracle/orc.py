@@ -42,7 +42,8 @@ class Opts(C.Structure):
                 ("mrw_gamma", C.c_float), ("mrw_tauthres", C.c_float),
                 ("mrw_count_trigger", C.c_int), ("max_interactions", C.c_int64),
                 ("nthreads", C.c_int), ("model_id", C.c_int), ("late_after", C.c_int64),
-                ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int)]
+                ("mrw_eager_after", C.c_int64), ("fp64_walls", C.c_int),
+                ("own_heating", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -170,7 +171,8 @@ def build_tables(lam_um, kabs, ksca, g, star_radius, star_temp):
 def mctherm(r_edges, th_edges, ph_edges, rho, lam_um, kabs, ksca, g, star_radius, star_temp,
             nphot, seed=0, nepoch=8, npilot=2, sequential=False, mrw=False, mrw_gamma=2.0,
             mrw_tauthres=10.0, mrw_count_trigger=100, max_interactions=10 ** 9, nthreads=0,
-            model_id=0, crossings=False, late_after=0, mrw_eager_after=0, fp64_walls=False):
+            model_id=0, crossings=False, late_after=0, mrw_eager_after=0, fp64_walls=False,
+            own_heating=1):
     """Run the oracle; returns dict(energy, temperature, escape, stats[, crossings])."""
     keep = _Keep()
     grid, dust, stars = _structs(r_edges, th_edges, ph_edges, lam_um, kabs, ksca, g,
@@ -184,7 +186,7 @@ def mctherm(r_edges, th_edges, ph_edges, rho, lam_um, kabs, ksca, g, star_radius
     cc = np.zeros(ncell, np.int64) if crossings else None
     opts = Opts(int(nphot), int(seed), nepoch, npilot, int(sequential), int(mrw), mrw_gamma,
                 mrw_tauthres, mrw_count_trigger, int(max_interactions), nthreads, model_id,
-                int(late_after), int(mrw_eager_after), int(bool(fp64_walls)))
+                int(late_after), int(mrw_eager_after), int(bool(fp64_walls)), int(own_heating))
     st = Stats()
     rc = lib().orc_mctherm(C.byref(grid), C.byref(dust), C.byref(stars),
                            rho.ctypes.data_as(C.c_void_p), C.byref(opts),

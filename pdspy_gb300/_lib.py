@@ -86,7 +86,8 @@ EXPORTS = [
     "pdgpu_mc_plan_create", "pdgpu_mc_plan_destroy", "pdgpu_mc_plan_layout",
     "pdgpu_mc_plan_upload", "pdgpu_mc_plan_run", "pdgpu_mc_plan_stats",
     "pdgpu_mctherm", "pdgpu_mctherm_workspace_bytes", "pdgpu_mc_plan_launch_ms",
-    "pdgpu_mc_plan_set_deadline",
+    "pdgpu_mc_plan_set_deadline", "pdgpu_mc_plan_set_model_deadlines",
+    "pdgpu_mc_plan_model_status",
     "pdgpu_image_plan_create", "pdgpu_image_plan_destroy", "pdgpu_image_plan_info",
     "pdgpu_image_plan_upload", "pdgpu_image_run", "pdgpu_image_adjoint", "pdgpu_image_flux",
     "pdgpu_vis_dft", "pdgpu_vis_dft_adjoint", "pdgpu_mctherm_static",
@@ -134,6 +135,10 @@ def lib(build_if_missing=True):
     L.pdgpu_mc_plan_launch_ms.argtypes = [vp, C.POINTER(C.c_float), i32]
     L.pdgpu_mc_plan_set_deadline.restype = i32
     L.pdgpu_mc_plan_set_deadline.argtypes = [vp, C.c_int64]
+    L.pdgpu_mc_plan_set_model_deadlines.restype = i32
+    L.pdgpu_mc_plan_set_model_deadlines.argtypes = [vp, vp, vp]
+    L.pdgpu_mc_plan_model_status.restype = i32
+    L.pdgpu_mc_plan_model_status.argtypes = [vp, vp, vp, vp]
     L.pdgpu_mctherm.restype = i32
     L.pdgpu_mctherm.argtypes = [i32, C.POINTER(ModelDesc), C.POINTER(DustDesc),
                                 C.POINTER(McOptions), vp, vp, vp, sz, vp, C.POINTER(McStats)]

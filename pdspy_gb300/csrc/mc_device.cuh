@@ -173,6 +173,53 @@ __device__ __forceinline__ void mc_rotate(float& kx, float& ky, float& kz, float
     kz = nz * rn;
 }
 
+// Energy a packet has deposited itself, per (species, cell), in a four-entry cache
+// (round-robin replacement).  The reemission temperature and the MRW mean opacities of a
+// cell are taken at the epoch's snapshot plus the packet's own deposits there: in
+// sequential Bjorkman & Wood a packet trapped in an optically thick cell heats the cell it
+// reemits from, and the epoch snapshot alone cannot see deposits made after it was taken.
+// The cache holds the last four cells, which covers a packet trapped at a wall or corner
+// between cells.  Keys are species * ncell + cell within the model; units are the int64
+// fixed-point deposits.  ver counts the deposits recorded (it keys per-cell caches of
+// values derived from the cell temperature).
+#define MC_OWN 4
+struct McOwn {
+    int32_t sc[MC_OWN];
+    long long u[MC_OWN];
+    int32_t next, ver;
+};
+
+__device__ __forceinline__ void own_init(McOwn& o) {
+#pragma unroll
+    for (int i = 0; i < MC_OWN; ++i) { o.sc[i] = -1; o.u[i] = 0; }
+    o.next = 0;
+    o.ver = 0;
+}
+
+__device__ __forceinline__ void own_add(McOwn& o, int sc, long long units) {
+    o.ver += 1;
+    bool hit = false;
+#pragma unroll
+    for (int i = 0; i < MC_OWN; ++i)
+        if (o.sc[i] == sc) { o.u[i] += units; hit = true; }
+    if (!hit) {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i)
+            if (i == o.next) { o.sc[i] = sc; o.u[i] = units; }
+        o.next = (o.next + 1) & (MC_OWN - 1);
+    }
+}
+
+// The packet's own deposits in (species, cell) sc as energy per gram per second:
+// (float) units * wq, with wq = (float)(q_unit / cell mass); 0 when not cached.
+__device__ __forceinline__ float own_q(const McOwn& o, int sc, float wq) {
+    long long u = 0;
+#pragma unroll
+    for (int i = 0; i < MC_OWN; ++i)
+        if (o.sc[i] == sc) u = o.u[i];
+    return u != 0 ? (float)u * wq : 0.0f;
+}
+
 // Upper bound of the distance to the nearest wall of the cell, kept along the walk: set
 // from a computed wall distance D (which is a lower bound within a relative 5e-6), grown
 // by every move (triangle inequality, rounded up), unknown after a crossing.

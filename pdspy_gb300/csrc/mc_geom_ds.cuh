@@ -92,7 +92,9 @@ struct PktS {
     McRng rng;
 };
 
-// Float-pool wall tables of one model.
+// Float-pool wall tables of one model.  The geometry below reads walls through the
+// accessors (sphere i: rh, r2; virtual cone j: mu, sn, mu2; phi half-plane k: cp, sp), so
+// a walk can also run on a copy of its current cell's walls held in registers (WallsCell).
 struct WallsS {
     const float *RH, *RL, *R2H, *R2L;    // sphere radii and squared radii (hi, lo)
     const float *MU, *SN, *MU2H, *MU2L;  // cone cos, sin and cos^2 (hi, lo), virtual index
@@ -101,8 +103,38 @@ struct WallsS {
         : RH(fg + M.off_rf), RL(fg + M.off_rl), R2H(fg + M.off_r2h), R2L(fg + M.off_r2l),
           MU(fg + M.off_muf), SN(fg + M.off_snf), MU2H(fg + M.off_mu2h), MU2L(fg + M.off_mu2l),
           CP(fg + M.off_cphf), SP(fg + M.off_sphf) {}
-    __device__ __forceinline__ ds R2(int i) const { return ds{R2H[i], R2L[i]}; }
-    __device__ __forceinline__ ds MU2(int j) const { return ds{MU2H[j], MU2L[j]}; }
+    __device__ __forceinline__ float rh(int i) const { return RH[i]; }
+    __device__ __forceinline__ ds r2(int i) const { return ds{R2H[i], R2L[i]}; }
+    __device__ __forceinline__ float mu(int j) const { return MU[j]; }
+    __device__ __forceinline__ float sn(int j) const { return SN[j]; }
+    __device__ __forceinline__ ds mu2(int j) const { return ds{MU2H[j], MU2L[j]}; }
+    __device__ __forceinline__ float cp(int k) const { return CP[k]; }
+    __device__ __forceinline__ float sp(int k) const { return SP[k]; }
+};
+
+// The walls of one cell (spheres ir and ir + 1, virtual cones itv and itv + 1, phi
+// half-planes ip and ip + 1) copied into registers; the accessors take the same indices
+// as WallsS and select the cached value, so the geometry computes identical results.
+struct WallsCell {
+    int i0, j0, k0;
+    float rh0, rh1, mu0, mu1, sn0, sn1, cp0, cp1, sp0, sp1;
+    ds r20, r21, mu20, mu21;
+    __device__ __forceinline__ void load(const WallsS& W, int ir, int itv, int ip, int np) {
+        i0 = ir; j0 = itv; k0 = ip;
+        if (ir >= 0) { rh0 = W.rh(ir); r20 = W.r2(ir); } else { rh0 = 0.0f; r20 = ds{0.0f, 0.0f}; }
+        rh1 = W.rh(ir + 1); r21 = W.r2(ir + 1);
+        mu0 = W.mu(itv); sn0 = W.sn(itv); mu20 = W.mu2(itv);
+        mu1 = W.mu(itv + 1); sn1 = W.sn(itv + 1); mu21 = W.mu2(itv + 1);
+        if (np > 1) { cp0 = W.cp(ip); sp0 = W.sp(ip); cp1 = W.cp(ip + 1); sp1 = W.sp(ip + 1); }
+        else { cp0 = sp0 = cp1 = sp1 = 0.0f; }
+    }
+    __device__ __forceinline__ float rh(int i) const { return i == i0 ? rh0 : rh1; }
+    __device__ __forceinline__ ds r2(int i) const { return i == i0 ? r20 : r21; }
+    __device__ __forceinline__ float mu(int j) const { return j == j0 ? mu0 : mu1; }
+    __device__ __forceinline__ float sn(int j) const { return j == j0 ? sn0 : sn1; }
+    __device__ __forceinline__ ds mu2(int j) const { return j == j0 ? mu20 : mu21; }
+    __device__ __forceinline__ float cp(int k) const { return k == k0 ? cp0 : cp1; }
+    __device__ __forceinline__ float sp(int k) const { return k == k0 ? sp0 : sp1; }
 };
 
 // Quantities shared by the wall candidates of one step.
@@ -112,7 +144,8 @@ struct FrameS {
     int last;
 };
 
-__device__ __forceinline__ void frame_ds(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ __forceinline__ void frame_ds(const McModel& M, const Wl& W, const PktS& p,
                                          FrameS& f) {
     f.x = p.x; f.y = p.y; f.z = p.z;
     f.kx = p.kx; f.ky = p.ky; f.kz = p.kz;
@@ -123,7 +156,7 @@ __device__ __forceinline__ void frame_ds(const McModel& M, const WallsS& W, cons
     f.b = ds_add(ds_add(ds_mulf(f.x, f.kx), ds_mulf(f.y, f.ky)), ds_mulf(f.z, f.kz));
     f.bf = f.b.h;
     f.last = p.last_wall;
-    float Ro = W.RH[(p.ir < 0) ? 0 : p.ir + 1];
+    float Ro = W.rh((p.ir < 0) ? 0 : p.ir + 1);
     f.tol = 1.0e-10f * Ro;
 }
 
@@ -137,9 +170,10 @@ __device__ __forceinline__ bool accept_root_s(float s, int wall, int last, float
 }
 
 // Coefficients of the cone quadric Q(s) = A s^2 + 2 B s + C = z(s)^2 - mu^2 r(s)^2.
-__device__ __forceinline__ void cone_coef(const WallsS& W, const FrameS& f, int w, float& A,
+template <class Wl>
+__device__ __forceinline__ void cone_coef(const Wl& W, const FrameS& f, int w, float& A,
                                           float& B, float& C) {
-    ds mu2 = W.MU2(w);
+    ds mu2 = W.mu2(w);
     A = f.kz * f.kz - mu2.h * f.kk;
     B = ds_sub(ds_mulf(f.z, f.kz), ds_mul(mu2, f.b)).h;
     C = ds_sub(f.z2, ds_mul(mu2, f.r2)).h;
@@ -147,13 +181,14 @@ __device__ __forceinline__ void cone_coef(const WallsS& W, const FrameS& f, int 
 
 // Exit distance through wall candidate k (0 outer sphere, 1 inner sphere, 2 lower cone,
 // 3 upper cone, 4 lower phi half-plane, 5 upper phi half-plane), before refinement.
-__device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ inline bool candidate_ds(const McModel& M, const Wl& W, const PktS& p,
                                     const FrameS& f, int k, float& out) {
     const float kk = f.kk, bf = f.bf, tol = f.tol;
     const int last = f.last;
     if (k == 0) {
         int io = (p.ir < 0) ? 0 : p.ir + 1;
-        float c = ds_sub(f.r2, W.R2(io)).h;
+        float c = ds_sub(f.r2, W.r2(io)).h;
         float D = bf * bf - kk * c;
         if (D < 0.0f) D = 0.0f;
         float sq = sqrtf(D);
@@ -165,7 +200,7 @@ __device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const Pkt
     if (p.ir < 0) return false;
     if (k == 1) {
         if (!(bf < 0.0f)) return false;
-        float c = ds_sub(f.r2, W.R2(p.ir)).h;
+        float c = ds_sub(f.r2, W.r2(p.ir)).h;
         float D = bf * bf - kk * c;
         if (!(D >= 0.0f)) return false;
         float s = c / (sqrtf(D) - bf);
@@ -176,7 +211,7 @@ __device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const Pkt
         int w = p.itv + side;
         if (w == 0 || w == M.ntv) return false;
         int code = side ? W_THI : W_TLO;
-        float mu = W.MU[w];
+        float mu = W.mu(w);
         float s = 0.0f;
         bool ok = false;
         if (mu == 0.0f) {
@@ -211,20 +246,20 @@ __device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const Pkt
     if (M.np <= 1) return false;
     if (k == 4) {
         int k0 = p.ip;
-        float g0 = ds_add(ds_mulf(f.x, -W.SP[k0]), ds_mulf(f.y, W.CP[k0])).h;
-        float dg = -f.kx * W.SP[k0] + f.ky * W.CP[k0];
+        float g0 = ds_add(ds_mulf(f.x, -W.sp(k0)), ds_mulf(f.y, W.cp(k0))).h;
+        float dg = -f.kx * W.sp(k0) + f.ky * W.cp(k0);
         if (!(dg < 0.0f)) return false;
         float s = -g0 / dg;
         float hx = f.x.h + s * f.kx, hy = f.y.h + s * f.ky;
-        return hx * W.CP[k0] + hy * W.SP[k0] > 0.0f && accept_root_s(s, W_PLO, last, tol, out);
+        return hx * W.cp(k0) + hy * W.sp(k0) > 0.0f && accept_root_s(s, W_PLO, last, tol, out);
     }
     int k1 = p.ip + 1;
-    float h0 = ds_add(ds_mulf(f.x, W.SP[k1]), ds_mulf(f.y, -W.CP[k1])).h;
-    float dh = f.kx * W.SP[k1] - f.ky * W.CP[k1];
+    float h0 = ds_add(ds_mulf(f.x, W.sp(k1)), ds_mulf(f.y, -W.cp(k1))).h;
+    float dh = f.kx * W.sp(k1) - f.ky * W.cp(k1);
     if (!(dh < 0.0f)) return false;
     float s = -h0 / dh;
     float hx = f.x.h + s * f.kx, hy = f.y.h + s * f.ky;
-    return hx * W.CP[k1] + hy * W.SP[k1] > 0.0f && accept_root_s(s, W_PHI, last, tol, out);
+    return hx * W.cp(k1) + hy * W.sp(k1) > 0.0f && accept_root_s(s, W_PHI, last, tol, out);
 }
 
 // One Newton step on the selected wall: the residual of the wall equation at x + s k in
@@ -233,7 +268,8 @@ __device__ inline bool candidate_ds(const McModel& M, const WallsS& W, const Pkt
 // is returned as a pair (s - correction): a single float cannot place the packet on the
 // wall (its spacing at 1e12 cm is 1e5 cm).  The result is >= 0.
 // Residual f and derivative f' of wall candidate k's equation at distance sd along the ray.
-__device__ __forceinline__ void wall_residual(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ __forceinline__ void wall_residual(const McModel& M, const Wl& W, const PktS& p,
                                               const FrameS& f, int k, ds sd, float& fv,
                                               float& fd) {
     const float s = sd.h;
@@ -243,35 +279,36 @@ __device__ __forceinline__ void wall_residual(const McModel& M, const WallsS& W,
     if (k == 0 || k == 1) {
         int i = (k == 1) ? p.ir : ((p.ir < 0) ? 0 : p.ir + 1);
         ds r2 = ds_add(ds_add(ds_sqr(X), ds_sqr(Y)), ds_sqr(Z));
-        fv = ds_sub(r2, W.R2(i)).h;
+        fv = ds_sub(r2, W.r2(i)).h;
         fd = 2.0f * (f.bf + s * f.kk);
     } else if (k == 2 || k == 3) {
         int w = p.itv + (k - 2);
-        if (W.MU[w] == 0.0f) {
+        if (W.mu(w) == 0.0f) {
             fv = Z.h;
             fd = f.kz;
         } else {
             float A, B, C;
             cone_coef(W, f, w, A, B, C);
             ds r2 = ds_add(ds_add(ds_sqr(X), ds_sqr(Y)), ds_sqr(Z));
-            fv = ds_sub(ds_sqr(Z), ds_mul(W.MU2(w), r2)).h;
+            fv = ds_sub(ds_sqr(Z), ds_mul(W.mu2(w), r2)).h;
             fd = 2.0f * (B + A * s);
         }
     } else if (k == 4) {
         int k0 = p.ip;
-        fv = ds_add(ds_mulf(X, -W.SP[k0]), ds_mulf(Y, W.CP[k0])).h;
-        fd = -f.kx * W.SP[k0] + f.ky * W.CP[k0];
+        fv = ds_add(ds_mulf(X, -W.sp(k0)), ds_mulf(Y, W.cp(k0))).h;
+        fd = -f.kx * W.sp(k0) + f.ky * W.cp(k0);
     } else {
         int k1 = p.ip + 1;
-        fv = ds_add(ds_mulf(X, W.SP[k1]), ds_mulf(Y, -W.CP[k1])).h;
-        fd = f.kx * W.SP[k1] - f.ky * W.CP[k1];
+        fv = ds_add(ds_mulf(X, W.sp(k1)), ds_mulf(Y, -W.cp(k1))).h;
+        fd = f.kx * W.sp(k1) - f.ky * W.cp(k1);
     }
 }
 
 // Newton refinement of candidate k's single-precision root s, the residual evaluated in
 // pairs.  A first correction larger than 1e-6 s (a near-tangent crossing, where the
 // single-precision root is poorly conditioned) is followed by a second step.
-__device__ inline ds refine_ds(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ inline ds refine_ds(const McModel& M, const Wl& W, const PktS& p,
                                const FrameS& f, int k, float s) {
     float fv, fd;
     wall_residual(M, W, p, f, k, ds{s, 0.0f}, fv, fd);
@@ -298,7 +335,8 @@ __device__ __forceinline__ int cand_wall_code(int k) {
 
 // Distance to the wall through which the packet leaves its cell: the first candidate (in
 // the order above) with the smallest exit distance, refined.
-__device__ inline ds next_wall_ds(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ inline ds next_wall_ds(const McModel& M, const Wl& W, const PktS& p,
                                   int& wall_out) {
     FrameS f;
     frame_ds(M, W, p, f);
@@ -322,26 +360,29 @@ __device__ inline ds next_wall_ds(const McModel& M, const WallsS& W, const PktS&
 
 // Virtual theta wall j lies at or below the packet's polar angle (cos theta_j >= z / r),
 // decided from the sign of z^2 - mu_j^2 r^2 in double-single.
-__device__ __forceinline__ bool mu_ge_ds(const WallsS& W, int j, const ds& z, const ds& z2,
+template <class Wl>
+__device__ __forceinline__ bool mu_ge_ds(const Wl& W, int j, const ds& z, const ds& z2,
                                          const ds& r2) {
-    float mu = W.MU[j];
-    float Q = ds_sub(z2, ds_mul(W.MU2(j), r2)).h;
+    float mu = W.mu(j);
+    float Q = ds_sub(z2, ds_mul(W.mu2(j), r2)).h;
     if (mu >= 0.0f) return z.h <= 0.0f || Q <= 0.0f;
     return z.h < 0.0f && Q >= 0.0f;
 }
 
 // Azimuth of the packet at or beyond phi wall k: the half-turn (sin phi < 0, or sin 0 and
 // cos < 0) and, within a half-turn, the sign of the plane function.
-__device__ __forceinline__ bool phi_ge_ds(const WallsS& W, int k, const ds& x, const ds& y) {
+template <class Wl>
+__device__ __forceinline__ bool phi_ge_ds(const Wl& W, int k, const ds& x, const ds& y) {
     int hp = (y.h < 0.0f || (y.h == 0.0f && x.h < 0.0f)) ? 1 : 0;
-    float sw = W.SP[k], cw = W.CP[k];
+    float sw = W.sp(k), cw = W.cp(k);
     int hw = (sw < 0.0f || (sw == 0.0f && cw < 0.0f)) ? 1 : 0;
     if (hp != hw) return hp > hw;
     return ds_add(ds_mulf(x, -sw), ds_mulf(y, cw)).h >= 0.0f;
 }
 
 // Angular cell of a packet entering the grid through its inner sphere.
-__device__ inline void locate_angles_ds(const McModel& M, const WallsS& W, PktS& p) {
+template <class Wl>
+__device__ inline void locate_angles_ds(const McModel& M, const Wl& W, PktS& p) {
     ds z2 = ds_sqr(p.z);
     ds r2 = ds_add(ds_add(ds_sqr(p.x), ds_sqr(p.y)), z2);
     int lo = 0, hi = M.ntv;
@@ -371,24 +412,25 @@ __device__ __forceinline__ int cell_of_s(const McModel& M, const PktS& p) {
 // distance and the MRW sphere radius).  The cancelling differences are formed in
 // double-single, the non-cancelling factors (r + R, |rho cos| + |z sin|) in single
 // precision; relative margin 4e-6.
-__device__ inline float wall_distance_ds(const McModel& M, const WallsS& W, const PktS& p) {
+template <class Wl>
+__device__ inline float wall_distance_ds(const McModel& M, const Wl& W, const PktS& p) {
     ds x2 = ds_sqr(p.x), y2 = ds_sqr(p.y), z2 = ds_sqr(p.z);
     ds rho2 = ds_add(x2, y2);
     ds r2 = ds_add(rho2, z2);
     float rf = sqrtf(r2.h);
-    float d = ds_sub(r2, W.R2(p.ir)).h / (rf + W.RH[p.ir]);
-    float d2 = ds_sub(W.R2(p.ir + 1), r2).h / (rf + W.RH[p.ir + 1]);
+    float d = ds_sub(r2, W.r2(p.ir)).h / (rf + W.rh(p.ir));
+    float d2 = ds_sub(W.r2(p.ir + 1), r2).h / (rf + W.rh(p.ir + 1));
     if (d2 < d) d = d2;
     float rhof = sqrtf(rho2.h);
     float zf = p.z.h;
     for (int side = 0; side < 2; ++side) {
         int w = p.itv + side;
         if (w == 0 || w == M.ntv) continue;
-        float a = rhof * W.MU[w];
-        float b = zf * W.SN[w];
+        float a = rhof * W.mu(w);
+        float b = zf * W.sn(w);
         float dt;
         if ((a > 0.0f) == (b > 0.0f)) {
-            float num = ds_sub(ds_mul(W.MU2(w), r2), z2).h;
+            float num = ds_sub(ds_mul(W.mu2(w), r2), z2).h;
             float den = fabsf(a) + fabsf(b);
             dt = den > 0.0f ? fabsf(num) / den : 0.0f;
         } else {
@@ -398,8 +440,8 @@ __device__ inline float wall_distance_ds(const McModel& M, const WallsS& W, cons
     }
     if (M.np > 1) {
         int k0 = p.ip, k1 = p.ip + 1;
-        float d0 = fabsf(ds_add(ds_mulf(p.x, -W.SP[k0]), ds_mulf(p.y, W.CP[k0])).h);
-        float d1 = fabsf(ds_add(ds_mulf(p.x, W.SP[k1]), ds_mulf(p.y, -W.CP[k1])).h);
+        float d0 = fabsf(ds_add(ds_mulf(p.x, -W.sp(k0)), ds_mulf(p.y, W.cp(k0))).h);
+        float d1 = fabsf(ds_add(ds_mulf(p.x, W.sp(k1)), ds_mulf(p.y, -W.cp(k1))).h);
         if (d0 < d) d = d0;
         if (d1 < d) d = d1;
     }
@@ -410,7 +452,8 @@ __device__ inline float wall_distance_ds(const McModel& M, const WallsS& W, cons
 // The same lower bound computed by a whole warp, one wall per lane (0 inner sphere, 1 outer
 // sphere, 2-3 cones, 4-5 phi half-planes) and reduced with min, which gives exactly the
 // value of wall_distance_ds.  Every lane returns the result.
-__device__ inline float wall_distance_ds_warp(const McModel& M, const WallsS& W, const PktS& p,
+template <class Wl>
+__device__ inline float wall_distance_ds_warp(const McModel& M, const Wl& W, const PktS& p,
                                               int lane) {
     float d = 3.0e38f;
     if (lane < 6) {
@@ -419,16 +462,16 @@ __device__ inline float wall_distance_ds_warp(const McModel& M, const WallsS& W,
         ds r2 = ds_add(rho2, z2);
         if (lane < 2) {
             float rf = sqrtf(r2.h);
-            if (lane == 0) d = ds_sub(r2, W.R2(p.ir)).h / (rf + W.RH[p.ir]);
-            else d = ds_sub(W.R2(p.ir + 1), r2).h / (rf + W.RH[p.ir + 1]);
+            if (lane == 0) d = ds_sub(r2, W.r2(p.ir)).h / (rf + W.rh(p.ir));
+            else d = ds_sub(W.r2(p.ir + 1), r2).h / (rf + W.rh(p.ir + 1));
         } else if (lane < 4) {
             int w = p.itv + (lane - 2);
             if (w != 0 && w != M.ntv) {
                 float rhof = sqrtf(rho2.h);
-                float a = rhof * W.MU[w];
-                float b = p.z.h * W.SN[w];
+                float a = rhof * W.mu(w);
+                float b = p.z.h * W.sn(w);
                 if ((a > 0.0f) == (b > 0.0f)) {
-                    float num = ds_sub(ds_mul(W.MU2(w), r2), z2).h;
+                    float num = ds_sub(ds_mul(W.mu2(w), r2), z2).h;
                     float den = fabsf(a) + fabsf(b);
                     d = den > 0.0f ? fabsf(num) / den : 0.0f;
                 } else {
@@ -438,10 +481,10 @@ __device__ inline float wall_distance_ds_warp(const McModel& M, const WallsS& W,
         } else if (M.np > 1) {
             if (lane == 4) {
                 int k0 = p.ip;
-                d = fabsf(ds_add(ds_mulf(p.x, -W.SP[k0]), ds_mulf(p.y, W.CP[k0])).h);
+                d = fabsf(ds_add(ds_mulf(p.x, -W.sp(k0)), ds_mulf(p.y, W.cp(k0))).h);
             } else {
                 int k1 = p.ip + 1;
-                d = fabsf(ds_add(ds_mulf(p.x, W.SP[k1]), ds_mulf(p.y, -W.CP[k1])).h);
+                d = fabsf(ds_add(ds_mulf(p.x, W.sp(k1)), ds_mulf(p.y, -W.cp(k1))).h);
             }
         }
     }

@@ -39,6 +39,7 @@
 #include <mutex>
 #include <new>
 #include <vector>
+#include <type_traits>
 
 #include "../../include/pdgpu.h"
 #include "mc_common.h"
@@ -54,12 +55,14 @@ using namespace pdgpu;
 // interaction count).  pos holds the position bits of either geometry.
 struct __align__(16) ParkRec {
     uint64_t pos[3];
+    long long own_u[MC_OWN];
     float dsafe, kx, ky, kz, tau;
     int ir, itv, ip, lam;
     int last_wall, cell_events, nevents, ncross;
     int m, epoch;
     uint32_t pid, model, tag, spare;   // spare: bits of dmax
-    int pad[3];
+    int own_sc[MC_OWN];
+    int own_next, own_ver, fresh, pad;
 };
 
 struct DustTabs {       // pointers into the staged (shared or global) dust tables
@@ -80,6 +83,7 @@ struct McParams {
     const McModel* models;
     const int64_t* cum;          // [nm+1] prefix of this epoch's packet counts
     const float* rho;            // [model][spec][cell]
+    const float* wq;             // [model][spec][cell] (float)(q_unit / cell mass)
     int64_t* E;                  // deposits of a packet's first late_after events
     int64_t* Elate;              // deposits of its later events
     const float2* q;             // (q_lo, q_span) per [epoch][model][spec][cell]
@@ -102,6 +106,9 @@ struct McParams {
     unsigned long long* queue;   // work counter of this launch
     const volatile int32_t* abort_flag;
     int64_t deadline_ns;
+    const int64_t* mdeadline;    // [nm] per-model deadline (ns from the run's start, 0 = none)
+    int32_t* mstat;              // [nm] per-model status (0 = running/ok, else why it stopped)
+    int32_t use_mdl;             // 1: per-model deadlines are set
     int64_t total;
     int32_t nm, ns, nl, epoch;
     uint32_t tag, key0, key1;
@@ -140,7 +147,11 @@ struct GeoS {
     }
     static __device__ __forceinline__ ds wall_warp(int lane, const McModel& M, const double*,
                                                    const float* fp, const Pkt& p, int& w) {
-        WallsS W(M, fp);
+        return wall_warp_w(lane, M, WallsS(M, fp), p, w);
+    }
+    template <class Wl>
+    static __device__ __forceinline__ ds wall_warp_w(int lane, const McModel& M, const Wl& W,
+                                                     const Pkt& p, int& w) {
         FrameS f;
         frame_ds(M, W, p, f);
         const int nk = (p.ir < 0) ? 1 : (M.np > 1 ? 6 : 4);
@@ -305,6 +316,48 @@ __device__ __forceinline__ MrwR mrw_of(uint4 b) {
 // and wall candidates and wall distances are computed one wall per lane.  Every result is
 // identical to the per-thread code; memory side effects are issued by lane 0.
 struct LanePol {
+    // the packet's own-deposit cache (McOwn) in shared memory, structure of arrays over the
+    // block's threads: keys [MC_OWN][nthr], units [MC_OWN][nthr], next [nthr]
+    int* osc;
+    long long* ou;
+    int* onext;
+    int tid, nthr;
+    __device__ __forceinline__ void own_reset() {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i) { osc[i * nthr + tid] = -1; ou[i * nthr + tid] = 0; }
+        onext[tid] = 0;
+    }
+    __device__ __forceinline__ void own_add(int sc, long long units) {
+        bool hit = false;
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i)
+            if (osc[i * nthr + tid] == sc) { ou[i * nthr + tid] += units; hit = true; }
+        if (!hit) {
+            const int nx = onext[tid];
+            osc[nx * nthr + tid] = sc;
+            ou[nx * nthr + tid] = units;
+            onext[tid] = (nx + 1) & (MC_OWN - 1);
+        }
+    }
+    __device__ __forceinline__ float own_q(int sc, float wq) const {
+        long long u = 0;
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i)
+            if (osc[i * nthr + tid] == sc) u = ou[i * nthr + tid];
+        return u != 0 ? (float)u * wq : 0.0f;
+    }
+    __device__ __forceinline__ int own_ver() const { return 0; }
+    __device__ __forceinline__ void own_save(ParkRec& r) const {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i) { r.own_sc[i] = osc[i * nthr + tid]; r.own_u[i] = ou[i * nthr + tid]; }
+        r.own_next = onext[tid];
+        r.own_ver = 0;
+    }
+    __device__ __forceinline__ void own_load(const ParkRec& r) {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i) { osc[i * nthr + tid] = r.own_sc[i]; ou[i * nthr + tid] = r.own_u[i]; }
+        onext[tid] = r.own_next;
+    }
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
         return mc_cdf_search(c, n, u);
     }
@@ -331,8 +384,13 @@ struct LanePol {
     __device__ __forceinline__ MrwR mrwd(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
         return mrw_of(mc_block(r, n, MC_RS_MRW, k0, k1));
     }
-    __device__ __forceinline__ bool cached(int, int, int, int) const { return false; }
-    __device__ __forceinline__ void remember(int, int, int, int, float) {}
+    __device__ __forceinline__ bool cached(int, int, int, int, int) const { return false; }
+    __device__ __forceinline__ void remember(int, int, int, int, int, float) {}
+    // q per deposit unit of species s in cell c (wq0 = the model's [spec][cell] block)
+    template <int NS>
+    __device__ __forceinline__ float wq(const float* wq0, int ncell, int, int c, int s) const {
+        return __ldg(wq0 + (int64_t)s * ncell + c);
+    }
     __device__ __forceinline__ float cached_value(int) const { return 0.0f; }
     __device__ __forceinline__ bool leader() const { return true; }
     // densities of cell c (rho0 = the model's [spec][cell] block)
@@ -356,12 +414,31 @@ struct WarpPol {
     EvR re;
     SecR rs;
     MrwR rm;
-    // per-cell cache: (model, cell, epoch) -> values by slot (Rosseland, Planck per species)
-    int cm, cc, ce;
+    // per-cell cache: (model, cell, epoch, own-deposit version) -> values by slot
+    // (Rosseland, Planck per species)
+    int cm, cc, ce, cv;
     unsigned cvalid;
     float cval[1 + MC_MAX_SPEC];
+    // the packet's own-deposit cache, replicated in every lane
+    McOwn own;
     __device__ __forceinline__ explicit WarpPol(int l)
-        : lane(l), rv(false), n0(0), cm(-1), cc(-1), ce(-1), cvalid(0u) {}
+        : lane(l), rv(false), n0(0), cm(-1), cc(-1), ce(-1), cv(-1), cvalid(0u) { own_init(own); }
+    __device__ __forceinline__ void own_reset() { own_init(own); }
+    __device__ __forceinline__ void own_add(int sc, long long units) { ::own_add(own, sc, units); }
+    __device__ __forceinline__ float own_q(int sc, float wq) const { return ::own_q(own, sc, wq); }
+    __device__ __forceinline__ int own_ver() const { return own.ver; }
+    __device__ __forceinline__ void own_save(ParkRec& r) const {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i) { r.own_sc[i] = own.sc[i]; r.own_u[i] = own.u[i]; }
+        r.own_next = own.next;
+        r.own_ver = own.ver;
+    }
+    __device__ __forceinline__ void own_load(const ParkRec& r) {
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i) { own.sc[i] = r.own_sc[i]; own.u[i] = r.own_u[i]; }
+        own.next = r.own_next;
+        own.ver = r.own_ver;
+    }
     // number of entries <= u of a non-decreasing table == smallest index with c > u
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
         int cnt = 0;
@@ -389,16 +466,36 @@ struct WarpPol {
             if (w > 1.0f) w = 1.0f;
         }
     }
+    // walls of the packet's current cell in registers (double-single geometry), reloaded
+    // when (ir, itv, ip) changes
+    int wir = -2, witv = -1, wip = -1;
+    WallsCell wcell;
+    __device__ __forceinline__ const WallsCell& cell_walls(const McModel& M, const float* fp,
+                                                           const PktS& p) {
+        if (p.ir != wir || p.itv != witv || p.ip != wip) {
+            wcell.load(WallsS(M, fp), p.ir, p.itv, p.ip, M.np);
+            wir = p.ir; witv = p.itv; wip = p.ip;
+        }
+        return wcell;
+    }
     template <class G>
     __device__ __forceinline__ typename G::len_t wall(const McModel& M, const double* dp,
                                                       const float* fp, const typename G::Pkt& p,
-                                                      int& w) const {
-        return G::wall_warp(lane, M, dp, fp, p, w);
+                                                      int& w) {
+        if constexpr (std::is_same<G, GeoS>::value) {
+            return G::wall_warp_w(lane, M, cell_walls(M, fp, p), p, w);
+        } else {
+            return G::wall_warp(lane, M, dp, fp, p, w);
+        }
     }
     template <class G>
     __device__ __forceinline__ float dist(const McModel& M, const double* dp, const float* fp,
-                                          const typename G::Pkt& p) const {
-        return G::dist_warp(lane, M, dp, fp, p);
+                                          const typename G::Pkt& p) {
+        if constexpr (std::is_same<G, GeoS>::value) {
+            return wall_distance_ds_warp(M, cell_walls(M, fp, p), p, lane);
+        } else {
+            return G::dist_warp(lane, M, dp, fp, p);
+        }
     }
     __device__ __forceinline__ int slot(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
         if (!rv || n < n0 || n - n0 >= 32u) {
@@ -439,20 +536,36 @@ struct WarpPol {
         o.jsn = __shfl_sync(0xffffffffu, rm.jsn, l);
         return o;
     }
-    __device__ __forceinline__ bool cached(int m, int c, int e, int k) const {
-        return cm == m && cc == c && ce == e && ((cvalid >> k) & 1u);
+    __device__ __forceinline__ bool cached(int m, int c, int e, int v, int k) const {
+        return cm == m && cc == c && ce == e && cv == v && ((cvalid >> k) & 1u);
     }
-    __device__ __forceinline__ void remember(int m, int c, int e, int k, float v) {
-        if (cm != m || cc != c || ce != e) { cm = m; cc = c; ce = e; cvalid = 0u; }
-        cval[k] = v;
+    __device__ __forceinline__ void remember(int m, int c, int e, int v, int k, float x) {
+        if (cm != m || cc != c || ce != e || cv != v) { cm = m; cc = c; ce = e; cv = v; cvalid = 0u; }
+        cval[k] = x;
         cvalid |= 1u << k;
     }
     __device__ __forceinline__ float cached_value(int k) const { return cval[k]; }
     __device__ __forceinline__ bool leader() const { return lane == 0; }
-    // densities and snapshots of the packet's cell, reloaded when the cell changes
-    int dm = -1, dc = -1, qm = -1, qc = -1, qe = -1;
+    // densities, q per deposit unit and snapshots of the packet's cell, reloaded when the
+    // cell changes
+    int dm = -1, dc = -1, qm = -1, qc = -1, qe = -1, wm = -1, wc = -1;
     float drho[MC_MAX_SPEC];
+    float dwq[MC_MAX_SPEC];
     float2 dq[MC_MAX_SPEC];
+    template <int NS>
+    __device__ __forceinline__ float wq(const float* wq0, int ncell, int m, int c, int s) {
+        if (m != wm || c != wc) {
+#pragma unroll
+            for (int k = 0; k < NS; ++k) dwq[k] = __ldg(wq0 + (int64_t)k * ncell + c);
+            wm = m;
+            wc = c;
+        }
+        float v = dwq[0];
+#pragma unroll
+        for (int k = 1; k < NS; ++k)
+            if (k == s) v = dwq[k];
+        return v;
+    }
     template <int NS>
     __device__ __forceinline__ void density(const float* rho0, int ncell, int m, int c, float* rh) {
         if (m != dm || c != dc) {
@@ -484,6 +597,7 @@ struct WarpPol {
 template <class Pol>
 __device__ __forceinline__ float row_interp(Pol& pol, const DustTabs& T, const float* tab, float q,
                                             int s) {
+    // q: the cell's energy per gram per second (mid-epoch snapshot + the packet's own)
     int j;
     float w;
     pol.row(T.F + s * MC_NROW, q, j, w);
@@ -494,8 +608,9 @@ __device__ __forceinline__ float row_interp(Pol& pol, const DustTabs& T, const f
 // three uniforms of the interaction's second stream.
 template <class Pol>
 __device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, float2 q, int s,
-                                             float uq, float urow, float ucdf) {
+                                             float uq, float urow, float ucdf, float own) {
     float qq = q.x + uq * q.y;
+    qq = qq + own;
     int j;
     float w;
     pol.row(T.F + s * MC_NROW, qq, j, w);
@@ -527,8 +642,8 @@ __device__ __forceinline__ void emit(typename G::Pkt& p, const DustTabs& T, cons
     p.ncross = 0;
 }
 
-template <class G>
-__device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p) {
+template <class G, class Pol>
+__device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p, const Pol& pol) {
     G::save(r, p);
     r.dsafe = p.dsafe;
     r.kx = p.kx; r.ky = p.ky; r.kz = p.kz; r.tau = p.tau;
@@ -537,11 +652,12 @@ __device__ __forceinline__ void park_save(ParkRec& r, const typename G::Pkt& p) 
     r.nevents = p.nevents; r.ncross = p.ncross; r.m = p.m; r.epoch = p.epoch;
     r.pid = p.rng.pid; r.model = p.rng.model; r.tag = p.rng.tag;
     r.spare = __float_as_uint(p.dmax);
-    r.pad[0] = p.fresh; r.pad[1] = 0; r.pad[2] = 0;
+    r.fresh = p.fresh; r.pad = 0;
+    pol.own_save(r);
 }
 
-template <class G>
-__device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r) {
+template <class G, class Pol>
+__device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r, Pol& pol) {
     G::load(p, r);
     p.dsafe = r.dsafe;
     p.kx = r.kx; p.ky = r.ky; p.kz = r.kz; p.tau = r.tau;
@@ -550,15 +666,16 @@ __device__ __forceinline__ void park_load(typename G::Pkt& p, const ParkRec& r) 
     p.nevents = r.nevents; p.ncross = r.ncross; p.m = r.m; p.epoch = r.epoch;
     p.rng.pid = r.pid; p.rng.model = r.model; p.rng.tag = r.tag;
     p.dmax = __uint_as_float(r.spare);
-    p.fresh = r.pad[0];
+    p.fresh = r.fresh;
+    pol.own_load(r);
 }
 
 // One transport step: a wall crossing or an interaction.  Returns false when the packet
 // has left the grid or was killed.
 template <int NS, class Pol, class G>
-__device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T, Cnt& cnt, Pol& pol) {
+__device__ __forceinline__ bool mc_step(typename G::Pkt& p, const McParams& P, const McModel& M,
+                                        const DustTabs& T, Cnt& cnt, Pol& pol) {
     using len_t = typename G::len_t;
-    const McModel& M = P.models[p.m];
     const double* __restrict__ dp = P.dpool;
     const int nl = P.nl;
     const uint32_t k0 = P.key0, k1 = P.key1;
@@ -629,13 +746,16 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
         if (cond && 0.999f * p.dmax * alpha >= P.mrw_tauthres) {
 #pragma unroll
             for (int s = 0; s < NS; ++s) qv[s] = pol.template snap<NS>(qa + base, M.ncell, p.m, c, p.epoch, s);
-            if (pol.cached(p.m, c, p.epoch, 0)) {
+            if (pol.cached(p.m, c, p.epoch, pol.own_ver(), 0)) {
                 aR = pol.cached_value(0);
             } else {
 #pragma unroll
-                for (int s = 0; s < NS; ++s)
-                    aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
-                pol.remember(p.m, c, p.epoch, 0, aR);
+                for (int s = 0; s < NS; ++s) {
+                    float qm = qv[s].x + 0.5f * qv[s].y;
+                    qm = qm + pol.own_q(s * M.ncell + c, pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, s));
+                    aR = aR + rh[s] * row_interp(pol, T, T.kR + s * MC_NROW, qm, s);
+                }
+                pol.remember(p.m, c, p.epoch, pol.own_ver(), 0, aR);
             }
             tried = 0.999f * p.dmax * aR >= P.mrw_gamma;
         }
@@ -658,19 +778,25 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 float aP = 0.0f;
 #pragma unroll
                 for (int s = 0; s < NS; ++s) {
-                    if (pol.cached(p.m, c, p.epoch, 1 + s)) {
+                    if (pol.cached(p.m, c, p.epoch, pol.own_ver(), 1 + s)) {
                         kp[s] = pol.cached_value(1 + s);
                     } else {
-                        kp[s] = rh[s] * row_interp(pol, T, T.kP + s * MC_NROW, qv[s].x + 0.5f * qv[s].y, s);
-                        pol.remember(p.m, c, p.epoch, 1 + s, kp[s]);
+                        float qm = qv[s].x + 0.5f * qv[s].y;
+                        qm = qm + pol.own_q(s * M.ncell + c,
+                                        pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, s));
+                        kp[s] = rh[s] * row_interp(pol, T, T.kP + s * MC_NROW, qm, s);
+                        pol.remember(p.m, c, p.epoch, pol.own_ver(), 1 + s, kp[s]);
                     }
                     aP = aP + kp[s];
                     float units_f = kp[s] * ell * 1048576.0f + 0.5f;
                     if (units_f > 9.0e18f) units_f = 9.0e18f;
                     long long units = (long long)units_f;
-                    if (units > 0 && pol.leader())
-                        atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
-                                  (unsigned long long)units);
+                    if (units > 0) {
+                        if (pol.leader())
+                            atomicAdd((unsigned long long*)(dep + base + (int64_t)s * M.ncell + c),
+                                      (unsigned long long)units);
+                        pol.own_add(s * M.ncell + c, units);
+                    }
                 }
                 float dx, dy, dz;
                 {
@@ -700,7 +826,8 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
 #pragma unroll
                 for (int s = 1; s < NS; ++s)
                     if (s == sp) qs = qv[s];
-                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf);
+                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf,
+                                      pol.own_q(sp * M.ncell + c, pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, sp)));
                 p.tau = ev.tn;
                 p.cell_events = 0;
                 cnt.mrw += 1;
@@ -755,8 +882,10 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
                 }
                 int64_t idx = base + (int64_t)sp * M.ncell + c;
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
+                pol.own_add(sp * M.ncell + c, 1ll << MC_EUNIT_SHIFT);
                 const float2 qs = pol.template snap<NS>(qa + base, M.ncell, p.m, c, p.epoch, sp);
-                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf);
+                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf,
+                                      pol.own_q(sp * M.ncell + c, pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, sp)));
                 {
                     float mu = 2.0f * ev.umu - 1.0f;
                     float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
@@ -782,7 +911,7 @@ __device__ bool mc_step(typename G::Pkt& p, const McParams& P, const DustTabs& T
             unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
             if ((long long)slot < P.park_out_cap) {
                 ParkRec r;
-                park_save<G>(r, p);
+                park_save<G>(r, p, pol);
                 P.park_out[slot] = r;
                 cnt.parked += 1;
                 return false;
@@ -835,8 +964,22 @@ __device__ __forceinline__ unsigned long long globaltimer() {
     return t;
 }
 
+// A model of a batched plan whose own deadline has passed is stopped: its status records
+// PDGPU_TIMEOUT, its remaining packets are dropped, and the other models go on (the
+// batched counterpart of one walker's radmc3d subprocess reaching its timelimit).
+__device__ __forceinline__ bool model_live(const McParams& P, int m) {
+    if (!P.use_mdl) return true;
+    if (*(volatile const int32_t*)(P.mstat + m) != 0) return false;
+    const long long dl = P.mdeadline[m];
+    if (dl > 0 && (long long)globaltimer() - *(volatile const long long*)(P.stats + ST_T0) > dl) {
+        atomicCAS(P.mstat + m, 0, (int32_t)PDGPU_TIMEOUT);
+        return false;
+    }
+    return true;
+}
+
 template <int NS, class G>
-__global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
+__global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
     int64_t* s_cum = reinterpret_cast<int64_t*>(sm + ((P.use_smem ? P.dust_floats : 0) + 3) / 4 * 4);
@@ -874,6 +1017,15 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
     bool active = false;
     unsigned iter = 0;
     LanePol lanepol;
+    {
+        // own-deposit caches of the block's threads, after the model prefix sums
+        char* ob = reinterpret_cast<char*>(s_cum + P.nm + 1);
+        lanepol.osc = reinterpret_cast<int*>(ob);
+        lanepol.ou = reinterpret_cast<long long*>(ob + (size_t)MC_OWN * blockDim.x * sizeof(int));
+        lanepol.onext = reinterpret_cast<int*>(ob + (size_t)MC_OWN * blockDim.x * (sizeof(int) + sizeof(long long)));
+        lanepol.tid = threadIdx.x;
+        lanepol.nthr = blockDim.x;
+    }
     bool queue_open = true;
     for (;;) {
         if (s_stop) break;
@@ -888,8 +1040,10 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
             if (!active) {
                 long long g = (long long)basev + __popc(need & lt_mask);
                 if (g < total) {
+                    bool live = true;
                     if (P.phase == 1) {
-                        park_load<G>(p, P.park_in[g]);
+                        park_load<G>(p, P.park_in[g], lanepol);
+                        live = model_live(P, p.m);
                     } else {
                         int lo = 0, hi = P.nm;
                         while (hi - lo > 1) {
@@ -902,10 +1056,14 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
                         p.rng.pid = (uint32_t)(M.bnd[P.epoch] + (g - s_cum[lo]));
                         p.rng.model = (uint32_t)M.model_id;
                         p.rng.tag = P.tag;
-                        emit<G>(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
+                        live = model_live(P, lo);
+                        if (live) {
+                            emit<G>(p, T, P.fpool + M.off_star, P.nl, P.key0, P.key1);
+                            lanepol.own_reset();
+                        }
                     }
-                    active = true;
-                    got = true;
+                    active = live;
+                    got = live;
                 }
             }
             if (P.phase == 1) {
@@ -913,10 +1071,15 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
                 if (lane == 0 && ng) atomicAdd(P.inflight, (unsigned long long)ng);
             }
         }
-        if (!__any_sync(0xffffffffu, active)) break;
+        if (!__any_sync(0xffffffffu, active)) {
+            if (!queue_open) break;
+            continue;   // every packet drawn belonged to stopped models: draw again
+        }
         const bool was = active;
+        // packets of a model that has reached its own deadline are dropped
+        if (active && P.use_mdl && (iter & 4095u) == 4095u && !model_live(P, p.m)) active = false;
         if (active) {
-            active = mc_step<NS, LanePol, G>(p, P, T, cnt, lanepol);
+            active = mc_step<NS, LanePol, G>(p, P, P.models[p.m], T, cnt, lanepol);
             if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
         }
         if (P.phase == 1) {
@@ -934,7 +1097,7 @@ __global__ void __launch_bounds__(256) mc_transport_kernel(McParams P) {
                         unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
                         if ((long long)slot < P.park_out_cap) {
                             ParkRec r;
-                            park_save<G>(r, p);
+                            park_save<G>(r, p, lanepol);
                             P.park_out[slot] = r;
                             parked = true;
                             active = false;
@@ -1027,11 +1190,15 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         g = __shfl_sync(0xffffffffu, g, 0);
         if ((long long)g >= total) break;
         typename G::Pkt p;
-        park_load<G>(p, P.park_in[g]);
         WarpPol pol(lane);
-        bool alive = true;
+        park_load<G>(p, P.park_in[g], pol);
+        // the packet's model, held in registers for the whole walk
+        const McModel Mw = P.models[p.m];
+        int live = 1;
+        if (lane == 0) live = model_live(P, p.m) ? 1 : 0;
+        bool alive = __shfl_sync(0xffffffffu, live, 0) != 0;
         while (alive) {
-            alive = mc_step<NS, WarpPol, G>(p, P, T, cnt, pol);
+            alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
                 if (lane == 0) {
@@ -1046,8 +1213,10 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
                         st = 1;
                     }
                     if (st) atomicExch((unsigned long long*)(P.stats + ST_STOP), 1ull);
+                    else if (!model_live(P, p.m)) st = 2;   // this packet's model stopped
                 }
                 st = __shfl_sync(0xffffffffu, st, 0);
+                if (st == 2) break;
                 if (st) { stop = true; break; }
             }
         }
@@ -1074,6 +1243,7 @@ struct PrepParams {
     const float* rho;
     const int64_t* src;       // energy the span is computed from
     float2* q;
+    float* wq;                // when set: (float)(q_unit / cell mass) per cell
     int64_t total;            // total cells over models and species
     int32_t nm, ns;
     int32_t first;            // 1: first epoch (q_lo = 0, q_span = src/m)
@@ -1105,6 +1275,7 @@ __global__ void mc_prep_kernel(PrepParams P) {
         const McModel& M = P.models[m];
         int c = (int)((i - M.cell_off) % M.ncell);
         double mass = cell_mass(M, P.dpool, P.rho[i], c);
+        if (P.wq) P.wq[i] = mass > 0.0 ? (float)(M.q_unit / mass) : 0.0f;
         float2 out = make_float2(0.0f, 0.0f);
         if (mass > 0.0) {
             double e = (double)P.src[i];
@@ -1192,7 +1363,9 @@ struct pdgpu_mc_plan {
     int64_t total_cells, total_nphot;
     // workspace layout
     size_t ws_fpool, ws_dpool, ws_models, ws_cum, ws_E, ws_D, ws_q, ws_escape, ws_stats,
-        ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_park2, ws_parkcnt;
+        ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_park2, ws_parkcnt, ws_wq,
+        ws_mdl, ws_mstat;
+    bool use_mdl;                   // per-model deadlines set (pdgpu_mc_plan_set_model_deadlines)
     int64_t park_cap;
     int nqueue;
     int device, nsm, block, grid;
@@ -1464,8 +1637,11 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     int smem_max = 0;
     if (P->device >= 0)
         cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->device);
-    P->smem_tables = (dust_bytes + cum_bytes + 64) <= (size_t)smem_max;
-    P->smem_bytes = (P->smem_tables ? dust_bytes : 0) + cum_bytes + 16;
+    // per-thread own-deposit caches of the per-thread transport launches
+    size_t own_bytes = (size_t)P->block * MC_OWN * (sizeof(int) + sizeof(long long)) +
+                       (size_t)P->block * sizeof(int);
+    P->smem_tables = (dust_bytes + cum_bytes + own_bytes + 64) <= (size_t)smem_max;
+    P->smem_bytes = (P->smem_tables ? dust_bytes : 0) + cum_bytes + own_bytes + 16;
     // workspace layout
     size_t o = 0;
     auto place = [&](size_t bytes) {
@@ -1483,6 +1659,7 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->ws_D = place((size_t)P->total_cells * sizeof(int64_t));
     P->ws_q = place((size_t)P->K * P->total_cells * sizeof(float2));
     P->ws_Elate = place((size_t)P->total_cells * sizeof(int64_t));
+    P->ws_wq = place((size_t)P->total_cells * sizeof(float));
     // room for every packet that outlives late_after in heavy-tailed runs (about 1 in 100
     // in the densest disks); a packet that finds the list full finishes in its epoch launch
     P->park_cap = std::max<int64_t>(65536, P->total_nphot / 16);
@@ -1492,6 +1669,9 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->ws_parkcnt = place(4 * sizeof(unsigned long long));
     P->ws_escape = place((size_t)nmodels * nl * sizeof(int64_t));
     P->ws_stats = place(MC_NSTAT * sizeof(int64_t));
+    P->ws_mdl = place((size_t)nmodels * sizeof(int64_t));
+    P->ws_mstat = place((size_t)nmodels * sizeof(int32_t));
+    P->use_mdl = false;
     P->nqueue = P->K + P->npilot + 2;   // one work counter per launch
     P->ws_queue = place((size_t)P->nqueue * sizeof(unsigned long long));
     P->ws_total = (o + 255) / 256 * 256;
@@ -1533,6 +1713,38 @@ pdgpu_status pdgpu_mc_plan_set_deadline(pdgpu_mc_plan* P, int64_t deadline_ns) {
     return PDGPU_OK;
 }
 
+pdgpu_status pdgpu_mc_plan_set_model_deadlines(pdgpu_mc_plan* P, const int64_t* deadline_ns,
+                                               void* stream) {
+    if (!P) return PDGPU_INVALID_ARG;
+    if (!P->uploaded_ws) return PDGPU_WORKSPACE;
+    std::vector<int64_t> d((size_t)P->nm, 0);
+    bool any = false;
+    if (deadline_ns)
+        for (int m = 0; m < P->nm; ++m) {
+            if (deadline_ns[m] < 0) return PDGPU_INVALID_ARG;
+            d[m] = deadline_ns[m];
+            any = any || d[m] > 0;
+        }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemcpyAsync((char*)P->uploaded_ws + P->ws_mdl, d.data(), d.size() * sizeof(int64_t),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    P->use_mdl = any;
+    return PDGPU_OK;
+}
+
+pdgpu_status pdgpu_mc_plan_model_status(pdgpu_mc_plan* P, const void* ws, void* stream,
+                                        int32_t* status) {
+    if (!P || !ws || !status) return PDGPU_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(status, (const char*)ws + P->ws_mstat, (size_t)P->nm * sizeof(int32_t),
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return PDGPU_CUDA_ERROR;
+    return PDGPU_OK;
+}
+
 pdgpu_status pdgpu_mc_plan_layout(const pdgpu_mc_plan* P, pdgpu_mc_layout* L) {
     if (!P || !L) return PDGPU_INVALID_ARG;
     L->tables_bytes = P->tables_bytes;
@@ -1562,8 +1774,10 @@ pdgpu_status pdgpu_mc_plan_upload(pdgpu_mc_plan* P, void* ws, size_t bytes, void
         cudaMemcpyAsync(w + P->ws_models, P->models.data(), P->models.size() * sizeof(McModel),
                         cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(w + P->ws_cum, P->cum.data(), P->cum.size() * sizeof(int64_t),
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_mdl, 0, (size_t)P->nm * sizeof(int64_t), st) != cudaSuccess)
         return PDGPU_CUDA_ERROR;
+    P->use_mdl = false;
     // pageable sources: make sure the copies finished before the host vectors can change
     if (cudaStreamSynchronize(st) != cudaSuccess) return PDGPU_CUDA_ERROR;
     P->uploaded_ws = ws;
@@ -1581,6 +1795,7 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.models = (const McModel*)(w + P->ws_models);
     prm.cum = (const int64_t*)(w + P->ws_cum) + (size_t)epoch * (P->nm + 1);
     prm.rho = rho;
+    prm.wq = (const float*)(w + P->ws_wq);
     prm.E = target;
     prm.Elate = final_pass ? (int64_t*)(w + P->ws_Elate) : target;
     prm.q = (const float2*)(w + P->ws_q);
@@ -1605,6 +1820,9 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.queue = (unsigned long long*)(w + P->ws_queue) + lslot;
     prm.abort_flag = P->opt.abort_flag;
     prm.deadline_ns = P->opt.deadline_ns;
+    prm.mdeadline = (const int64_t*)(w + P->ws_mdl);
+    prm.mstat = (int32_t*)(w + P->ws_mstat);
+    prm.use_mdl = P->use_mdl ? 1 : 0;
     prm.total = phase == 0 ? P->cum[(size_t)epoch * (P->nm + 1) + P->nm] : P->park_cap;
     if (phase == 1 && P->opt.drain_below >= 0) {
         int64_t d = P->opt.drain_below;
@@ -1696,6 +1914,7 @@ static pdgpu_status launch_prep(pdgpu_mc_plan* P, char* w, const float* rho, con
     q.rho = rho;
     q.src = src;
     q.q = (float2*)(w + P->ws_q) + (size_t)epoch * P->total_cells;
+    q.wq = (first && epoch == 0) ? (float*)(w + P->ws_wq) : nullptr;
     q.total = P->total_cells;
     q.nm = P->nm;
     q.ns = P->ns;
@@ -1723,6 +1942,7 @@ pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* P, const float* rho, double* tempe
         cudaMemsetAsync(w + P->ws_parkcnt, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_escape, 0, (size_t)P->nm * P->nl * sizeof(int64_t), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_stats, 0, MC_NSTAT * sizeof(int64_t), st) != cudaSuccess ||
+        cudaMemsetAsync(w + P->ws_mstat, 0, (size_t)P->nm * sizeof(int32_t), st) != cudaSuccess ||
         cudaMemsetAsync(w + P->ws_queue, 0, (size_t)P->nqueue * sizeof(unsigned long long), st) !=
             cudaSuccess)
         return PDGPU_CUDA_ERROR;

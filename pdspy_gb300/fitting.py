@@ -198,6 +198,9 @@ def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=N
     """lnprob of every walker (rows of P, the free parameters in sorted key order as
     pdspy's lnprob orders them) with one batched thermal launch; returns float64 [nwalker].
 
+    timelimit: seconds of device time per walker (one number or one per row of P); a
+    walker whose thermal run has not finished in time scores -inf alone.
+
     visibilities: list of dicts with "data" (vis.UVData plus ``freq``), "npix" and
     "pixelsize" (arcsec), one per visibility set (pdspy's visibilities["data"][j],
     ["npix"][j], ["pixelsize"][j])."""
@@ -221,12 +224,19 @@ def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=N
         lps.append(lp)
     if not models:
         return out
+    # each walker has its own time limit (run_disk_model.py:251-273): a walker that runs out
+    # of time scores -inf alone (utils/emcee.py:22-23), the others are scored as usual
+    limits = timelimit
+    if limits is not None and np.ndim(limits) > 0:
+        limits = [np.asarray(limits, dtype=object)[w] for w in live]   # one per walker of P
     try:
-        thermal.run_thermal_batched(models, nphot=nphot, iseed=seed, timelimit=timelimit,
+        thermal.run_thermal_batched(models, nphot=nphot, iseed=seed, model_timelimit=limits,
                                     **THERMAL)
     except subprocess.TimeoutExpired:
         return out
     for w, m, p, lp in zip(live, models, res, lps):
+        if m.grid.temperature is None:
+            continue
         ll = 0.0
         for j, vs in enumerate(visibilities):
             vs = dict(vs, index=j + 1)

@@ -29,7 +29,7 @@ _IGNORED = {"setthreads", "nice", "verbose", "nphot_scat", "nphot_spec", "incl_d
             "scattering_mode_max", "istar_sphere", "itempdecoup"}
 
 DEFAULTS = dict(nepoch=8, npilot=2, mrw_gamma=2.0, mrw_tauthres=10.0, mrw_count_trigger=100,
-                max_interactions=2_000_000_000, late_after=10000, mrw_eager_after=10000)
+                max_interactions=2_000_000_000, late_after=100000, mrw_eager_after=10000)
 
 
 def _dptr(a):
@@ -252,6 +252,32 @@ class ThermalPlan:
         _lib.check(self.L.pdgpu_mc_plan_set_deadline(self._plan, ns), "pdgpu_mc_plan_set_deadline")
         self.timelimit = seconds
 
+    def set_model_timelimits(self, seconds):
+        """Per-model device-clock budgets (s) of the following runs: a sequence with one entry
+        per model (None or 0: no limit), one number for every model, or None to clear.  A
+        model that has not finished in time stops with status 2 (timeout) and the others
+        finish unchanged (run_disk_model.py:251-273 times out each walker on its own)."""
+        if seconds is None:
+            arr = None
+        else:
+            sec = np.broadcast_to(np.asarray([0.0 if x is None else float(x) for x in
+                                              np.atleast_1d(np.asarray(seconds, dtype=object))]),
+                                  (self.nmodels,))
+            arr = np.ascontiguousarray(np.round(sec * 1e9).astype(np.int64))
+        stream = torch.cuda.current_stream(self.device)
+        _lib.check(self.L.pdgpu_mc_plan_set_model_deadlines(
+            self._plan, None if arr is None else arr.ctypes.data, stream.cuda_stream),
+            "pdgpu_mc_plan_set_model_deadlines")
+
+    def model_status(self):
+        """Status of every model after the last run: int32 array (0 ok, 2 timed out)."""
+        out = np.zeros(self.nmodels, dtype=np.int32)
+        stream = torch.cuda.current_stream(self.device)
+        _lib.check(self.L.pdgpu_mc_plan_model_status(self._plan, self.workspace.data_ptr(),
+                                                     stream.cuda_stream, out.ctypes.data),
+                   "pdgpu_mc_plan_model_status")
+        return out
+
     def launch_ms(self):
         """CUDA-event durations (ms) of the last run's transport launches."""
         buf = (C.c_float * 32)()
@@ -357,10 +383,19 @@ def run_thermal(model, nphot=1e6, **keywords):
     return stats
 
 
-def run_thermal_batched(models, nphot=1e6, **keywords):
-    """Thermal runs of many models (e.g. MCMC walkers) in one persistent launch per epoch."""
+def run_thermal_batched(models, nphot=1e6, model_timelimit=None, **keywords):
+    """Thermal runs of many models (e.g. MCMC walkers) in one persistent launch per epoch.
+
+    ``timelimit`` bounds the whole launch (every model times out together and
+    subprocess.TimeoutExpired is raised, as for one model).  ``model_timelimit`` (seconds,
+    one number or one per model) is the per-walker limit of run_disk_model.py:251-273: a
+    model that has not finished in time is stopped alone; its ``grid.temperature`` is set
+    to None and its entry of ``stats["model_status"]`` is 2, while the others finish with
+    the results they have without the limit."""
     opts = _options(keywords)
     plan = ThermalPlan([m.grid for m in models], nphot, **opts)
+    if model_timelimit is not None:
+        plan.set_model_timelimits(model_timelimit)
     rho_h = torch.from_numpy(np.concatenate([stack_density(m.grid).reshape(-1) for m in models])
                              ).pin_memory()
     rho, T = plan.new_buffers()
@@ -369,8 +404,10 @@ def run_thermal_batched(models, nphot=1e6, **keywords):
     Th = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
     Th.copy_(T, non_blocking=True)
     stats = plan.check_status()
-    for m, temps in zip(models, plan.split(Th)):
-        m.grid.temperature = temps
+    status = plan.model_status()
+    stats["model_status"] = [int(x) for x in status]
+    for m, temps, st in zip(models, plan.split(Th), status):
+        m.grid.temperature = temps if st == 0 else None
     return stats
 
 

@@ -65,3 +65,35 @@ def image_model(kind="disk", nr=16, ntheta=16, nphi=1, mass=1e-3, lam=None):
     T = 150.0 * rr ** -0.5
     g.temperature = [T * (1.0 + 0.1 * i) for i in range(len(g.density))]
     return m
+
+
+def _pool_run(args):
+    """One single-threaded oracle run (worker of oracle_ensemble): (temperature, crossings)."""
+    builder, bkw, nphot, seed, kw = args
+    from pdspy_gb300 import workloads as w
+    m = getattr(w, builder)(**bkw)
+    r = run_oracle(m, nphot, seed=seed, crossings=True, nthreads=1, **kw)
+    return r["temperature"], r["crossings"]
+
+
+def oracle_ensemble(builder, bkw, nphot, seeds, workers=8, **kw):
+    """Oracle runs of workloads.<builder>(**bkw) for each seed, in a spawn-started process
+    pool.  Returns (temperatures [seed][spec][nr][nt][np], summed crossings)."""
+    import multiprocessing as mp
+    args = [(builder, bkw, nphot, int(s), kw) for s in seeds]
+    with mp.get_context("spawn").Pool(min(workers, len(args))) as pool:
+        res = pool.map(_pool_run, args)
+    return np.array([r[0] for r in res]), np.sum([r[1] for r in res], axis=0)
+
+
+def four_sigma(T_a, T_b, crossings, min_crossings=1000):
+    """Per-cell comparison of two ensembles (spec criterion): z = difference of the
+    seed means over its standard error, on cells crossed >= min_crossings times per run with
+    a positive mean temperature in both ensembles.  Returns (z, relative difference of the
+    means) on those cells."""
+    na, nb = len(T_a), len(T_b)
+    ma, mb = T_a.mean(0), T_b.mean(0)
+    sig = np.sqrt(T_a.var(0, ddof=1) / na + T_b.var(0, ddof=1) / nb)
+    C = np.broadcast_to(crossings / na, ma.shape)
+    sel = (C >= min_crossings) & (ma > 0) & (mb > 0) & (sig > 0)
+    return (ma - mb)[sel] / sig[sel], (ma - mb)[sel] / mb[sel]

@@ -1,9 +1,9 @@
 """Generate golden fixtures from the reference pdspy's own density builders.
 
-Run in a container where the pdspy sources are available (default location below, or
-PDSPY_SOURCE=<path to the pdspy checkout>):
+Run where a pdspy source checkout is available, naming it on the command line or in
+PDSPY_SOURCE:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path to the pdspy checkout>
 
 pdspy cannot be imported as a package here (pdspy/__init__.py imports every subpackage,
 some of which need h5py, compiled Cython modules and scipy.integrate.trapz, removed in
@@ -22,7 +22,17 @@ import numpy as np
 import scipy.integrate
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.environ.get("PDSPY_SOURCE", "/root/reference")
+SRC = None
+
+
+def source_dir(argv=None):
+    """The pdspy checkout: the first command-line argument, else $PDSPY_SOURCE."""
+    argv = sys.argv[1:] if argv is None else argv
+    src = argv[0] if argv else os.environ.get("PDSPY_SOURCE")
+    if not src or not os.path.isfile(os.path.join(src, "pdspy", "modeling", "Disk.py")):
+        raise SystemExit("usage: make_golden.py <pdspy checkout> (or set PDSPY_SOURCE); "
+                         "got %r" % (src,))
+    return src
 
 
 def _shim():
@@ -60,6 +70,8 @@ def _shim():
 
 
 def main():
+    global SRC
+    SRC = source_dir()
     star, disk, env, const = _shim()
     out = {}
     # small axisymmetric disk on 100 log-r cells over 0.1-100 au and 100 theta cells over [0, pi]

@@ -46,3 +46,37 @@ def test_abort_flag_stops_the_run(cuda):
     plan.run(rho, T)
     st = plan.check_status()
     assert st["status"] == 0 and st["packets"] == 20000
+
+
+def test_one_walker_timeout_leaves_the_others_unchanged(cuda):
+    """A batched plan with a per-model limit: the walker whose limit is 1 ns stops alone
+    (status 2, its packets dropped); every other walker's energies and temperatures are
+    bit for bit those of the same plan run without limits."""
+    from pdspy_gb300 import workloads
+    models = workloads.walker_models(n=4, seed=8, scale=0.2)
+    plan = thermal.ThermalPlan([m.grid for m in models], 3000, seed=4, mrw=True,
+                               mrw_count_trigger=10)
+    rho, T = plan.new_buffers()
+    rho.copy_(torch.from_numpy(np.concatenate([thermal.stack_density(m.grid).reshape(-1)
+                                               for m in models])))
+    plan.run(rho, T)
+    plan.check_status()
+    assert list(plan.model_status()) == [0, 0, 0, 0]
+    E0, T0 = plan.energy().clone(), T.clone()
+    plan.set_model_timelimits([None, 1e-9, None, 3600.0])
+    plan.run(rho, T)
+    st = plan.check_status()                       # the launch as a whole completes
+    assert st["status"] == 0
+    assert list(plan.model_status()) == [0, 2, 0, 0]
+    off = 0
+    for i, (ns, nr, nt, np_) in enumerate(plan.shapes):
+        n = ns * nr * nt * np_
+        if i != 1:
+            assert torch.equal(plan.energy()[off:off + n], E0[off:off + n]), i
+            assert torch.equal(T[off:off + n], T0[off:off + n]), i
+        off += n
+    plan.set_model_timelimits(None)               # cleared: every walker finishes again
+    plan.run(rho, T)
+    plan.check_status()
+    assert list(plan.model_status()) == [0, 0, 0, 0]
+    assert torch.equal(plan.energy(), E0) and torch.equal(T, T0)

@@ -52,3 +52,9 @@ def test_lnprob_batched_orders_walkers(cuda):
     assert lp[0] == pytest.approx(best, rel=1e-12)  # the data's own model: chi^2 = 0
     assert np.isfinite(lp[1]) and np.isfinite(lp[3])
     assert lp[1] < lp[0] and lp[3] < lp[0]
+    # a per-walker time limit: walker 3 runs out of time alone and scores -inf; the other
+    # walkers' values are unchanged bit for bit
+    lp2 = fitting.lnprob_batched(walkers, sets, P, dust=dust, lam_um=lam, nphot=20000, seed=5,
+                                 device=cuda, timelimit=[3600.0, 3600.0, 3600.0, 1e-9])
+    assert lp2[3] == -np.inf and lp2[2] == -np.inf
+    assert lp2[0] == lp[0] and lp2[1] == lp[1]

@@ -5,7 +5,7 @@ pdgpu_mctherm_static serves callers that cannot allocate device memory (their GP
 belongs to another runtime or pool); it keeps its workspace in a static device array inside
 the library.  Both entry points run the same algorithm on the same random streams, so their
 temperatures and counters must be identical, on every call: the static array keeps the last
-call's contents, and each run must clear what it accumulates.  This file is collected last
+call's contents, and each run must clear what it accumulates, whatever ran before it.  This file is collected last
 so that a failure here cannot hide another test's result.
 """
 import ctypes as C
@@ -19,7 +19,7 @@ from pdspy_gb300 import _lib, thermal, workloads
 pytestmark = pytest.mark.gpu
 
 
-def _descriptors(models, nphot, keep):
+def _descriptors(models, nphot, keep, late_after=200, seed=5):
     def arr(a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         keep.append(a)
@@ -38,9 +38,9 @@ def _descriptors(models, nphot, keep):
         ka.append(a); ks.append(s); gg.append(np.zeros_like(a) if gv is None else gv)
     dust = _lib.DustDesc(len(g.lam), len(g.dust), arr(g.lam), arr(np.stack(ka)),
                          arr(np.stack(ks)), arr(np.stack(gg)))
-    opts = _lib.McOptions(seed=5, nepoch=8, npilot=2, mrw=1, mrw_gamma=2.0, mrw_tauthres=10.0,
-                          mrw_count_trigger=20, max_interactions=2_000_000_000, late_after=200,
-                          mrw_eager_after=200)
+    opts = _lib.McOptions(seed=seed, nepoch=8, npilot=2, mrw=1, mrw_gamma=2.0, mrw_tauthres=10.0,
+                          mrw_count_trigger=20, max_interactions=2_000_000_000,
+                          late_after=late_after, mrw_eager_after=late_after)
     return descs, dust, opts
 
 
@@ -49,32 +49,54 @@ def _rho(models, dev):
                                            for m in models]), device=dev)
 
 
-def test_static_entry_point_matches_workspace_entry_point(cuda):
-    L = _lib.lib()
-    models = workloads.walker_models(n=2, seed=3, scale=0.12)
-    keep = []
-    descs, dust, opts = _descriptors(models, 6000, keep)
-    rho = _rho(models, cuda)
-    n = rho.numel()
-    stream = torch.cuda.current_stream(cuda).cuda_stream
-    # existing entry point with a caller-allocated workspace
+def _workspace_run(L, models, descs, dust, opts, rho, stream, dev):
+    """pdgpu_mctherm with a caller-allocated workspace: the expected result."""
     nbytes = L.pdgpu_mctherm_workspace_bytes(len(models), descs, C.byref(dust), C.byref(opts))
-    ws = torch.empty(nbytes, dtype=torch.uint8, device=cuda)
-    T_ref = torch.empty(n, dtype=torch.float64, device=cuda)
-    st_ref = _lib.McStats()
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    T = torch.empty(rho.numel(), dtype=torch.float64, device=dev)
+    st = _lib.McStats()
     assert L.pdgpu_mctherm(len(models), descs, C.byref(dust), C.byref(opts), rho.data_ptr(),
-                           T_ref.data_ptr(), ws.data_ptr(), nbytes, stream,
-                           C.byref(st_ref)) == 0
-    assert st_ref.parked > 0        # the continuation path runs too
-    for call in range(2):
-        T = torch.full((n,), -1.0, dtype=torch.float64, device=cuda)
-        st = _lib.McStats()
-        rc = L.pdgpu_mctherm_static(len(models), descs, C.byref(dust), C.byref(opts),
-                                    rho.data_ptr(), T.data_ptr(), stream, C.byref(st))
-        assert rc == 0, _lib.STATUS.get(rc)
-        torch.cuda.synchronize(cuda)
+                           T.data_ptr(), ws.data_ptr(), nbytes, stream, C.byref(st)) == 0
+    return T, st
+
+
+def _static_run(L, models, descs, dust, opts, rho, stream, dev):
+    T = torch.full((rho.numel(),), -1.0, dtype=torch.float64, device=dev)
+    st = _lib.McStats()
+    rc = L.pdgpu_mctherm_static(len(models), descs, C.byref(dust), C.byref(opts),
+                                rho.data_ptr(), T.data_ptr(), stream, C.byref(st))
+    assert rc == 0, _lib.STATUS.get(rc)
+    torch.cuda.synchronize(dev)
+    return T, st
+
+
+def test_static_entry_point_matches_workspace_entry_point(cuda):
+    """Two static calls of one workload with a different workload between them (three
+    models, another packet count and park limit, so its tables, queues and parked packets
+    reach past the first workload's offsets): each call equals pdgpu_mctherm bit for bit."""
+    L = _lib.lib()
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    keep = []
+    models_a = workloads.walker_models(n=2, seed=3, scale=0.12)
+    a = _descriptors(models_a, 6000, keep)
+    rho_a = _rho(models_a, cuda)
+    models_b = workloads.walker_models(n=3, seed=9, scale=0.18)
+    b = _descriptors(models_b, 9000, keep, late_after=80, seed=17)
+    rho_b = _rho(models_b, cuda)
+    T_a, st_a = _workspace_run(L, models_a, *a, rho_a, stream, cuda)
+    T_b, st_b = _workspace_run(L, models_b, *b, rho_b, stream, cuda)
+    assert st_a.parked > 0 and st_b.parked > 0   # the continuation path runs too
+    assert rho_b.numel() > rho_a.numel()
+    for call, (models, d, rho, T_ref, st_ref) in enumerate(
+            [(models_a, a, rho_a, T_a, st_a), (models_b, b, rho_b, T_b, st_b),
+             (models_a, a, rho_a, T_a, st_a)]):
+        T, st = _static_run(L, models, *d, rho, stream, cuda)
         assert torch.equal(T, T_ref), call
-        assert st.asdict() == st_ref.asdict(), call
+        # every counter of the walk; "drained" counts how many resumed packets were handed
+        # to the one-per-warp stage, which depends on timing, not on the result
+        got, want = st.asdict(), st_ref.asdict()
+        got.pop("drained"), want.pop("drained")
+        assert got == want, call
 
 
 def test_static_entry_point_rejects_runs_beyond_its_scratch(cuda):
