@@ -131,6 +131,22 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
+def cpu_model():
+    """Host CPU model string and thread count (lscpu's model name, else platform)."""
+    import platform
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"model": name or platform.processor() or platform.machine(),
+            "threads": os.cpu_count(), "machine": platform.machine()}
+
+
 def max_over_ranks(v, world, device=None):
     """The maximum of v over all ranks (every rank's timed region ends at the slowest)."""
     if world <= 1:
@@ -408,8 +424,12 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     models = build_models(args, rank)
-    plan = thermal.ThermalPlan([m.grid for m in models], args.packets, seed=args.seed,
-                               time_launches=True, timelimit=args.timelimit, **MRW)
+    # one plan per timed step: step k runs the same models with Monte Carlo seed seed + k, so
+    # the steps sample the heavy tail of the walk lengths instead of repeating one draw
+    plans = [thermal.ThermalPlan([m.grid for m in models], args.packets, seed=args.seed + k,
+                                 time_launches=True, timelimit=args.timelimit, **MRW)
+             for k in range(max(args.steps, 1))]
+    plan = plans[0]
     host_rho = torch.from_numpy(np.concatenate(
         [thermal.stack_density(m.grid).reshape(-1) for m in models])).pin_memory()
     rho, T = plan.new_buffers()
@@ -438,7 +458,8 @@ def main():
     # temperatures, event d.  value uses b..c (inputs resident in HBM), e2e uses a..d.
     step_ms, e2e_ms, launch_ms, launch_stats, stats = [], [], [], [], []
     with Clocks(local) as clk:
-        for _ in range(args.steps):
+        for k in range(args.steps):
+            plan = plans[k]
             flush.zero_()
             barrier()
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -456,6 +477,18 @@ def main():
             launch_stats.append(plan.launch_stats())
             stats.append(plan.check_status())
 
+    # per step: the warp-per-packet stage (the last transport launch: the longest walks) and
+    # everything before it
+    tail_ms = [lm[-1] if lm else 0.0 for lm in launch_ms]
+    bulk_ms = [a - b for a, b in zip(step_ms, tail_ms)]
+    seeds = {"mc_seeds": [args.seed + k for k in range(args.steps)],
+             "ms_per_step": [round(x, 1) for x in step_ms],
+             "median_ms": float(np.median(step_ms)), "min_ms": float(np.min(step_ms)),
+             "max_ms": float(np.max(step_ms)),
+             "bulk_ms": [round(x, 1) for x in bulk_ms],
+             "tail_ms": [round(x, 1) for x in tail_ms],
+             "longest_walk": [max([b for (_, b, _) in ls] or [0]) for ls in launch_stats],
+             "events": [int(st_["events"]) for st_ in stats]}
     t_max = max_over_ranks(float(np.sum(step_ms)), world, dev)
     te = max_over_ranks(float(np.sum(e2e_ms)), world, dev)
     value = weak_scaling_rate(world, total_packets, args.steps, t_max)
@@ -485,14 +518,22 @@ def main():
         except Exception:
             traffic = None
     achieved = (alg_bytes / n_launch) / (avg_launch / 1e3) / 1e9
+    events_all = float(np.sum([st_["events"] for st_ in stats]))
+    t_bulk = max_over_ranks(float(np.sum(bulk_ms)), world, dev)
+    interactions = {"per_s": world * events_all / (t_max / 1e3),
+                    "bulk_per_s": world * events_all / (t_bulk / 1e3) if t_bulk > 0 else None,
+                    "note": "interactions (absorptions, scatterings, MRW steps) per second over the "
+                            "timed steps; bulk_per_s divides by the time before the "
+                            "warp-per-packet stage"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "kernel": "mc_transport_kernel + mc_continue_kernel (every walk launch)",
                 "peak_source": "measured" if peaks else "fallback",
                 "traffic_source": "null: ncu DRAM bytes per walk launch are 0.26-0.35 MB on the "
                                   "plain disk (profiles/), the working set stays in L2",
-                "launches_per_step": n_launch, "kernel_ms_per_step": float(np.sum(lm)),
-                "algorithmic_bytes_per_step": int(alg_bytes)}
+                "launches_per_step": n_launch,
+                "walk_kernel_ms_last_step": float(np.sum(lm)),
+                "algorithmic_bytes_last_step": int(alg_bytes)}
 
     adj = None
     if rank == 0 and not args.no_adjoint:
@@ -537,6 +578,7 @@ def main():
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "adjoint": adj,
                 "scattering": scat, "lnprob": lnp, "visibility_sampling": vrate,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+                "seeds": seeds, "interactions": interactions, "host_cpu": cpu_model(),
                 "stats": {k: st[k] for k in ("events", "crossings", "absorptions", "mrw_steps",
                                             "parked", "drained", "killed", "late_units")},
                 "launch_ms": [round(x, 3) for x in launch_ms[-1]],

@@ -119,6 +119,8 @@ struct McParams {
     int32_t dust_floats, use_smem;
     int32_t o_kabs, o_ksca, o_kext, o_g, o_F, o_cdf, o_kP, o_kR, o_mrw;
     int32_t count_stats;
+    int32_t g_const;             // 1: every species has the one asymmetry g0 at every wavelength
+    float g0;
 };
 
 struct Cnt {
@@ -305,6 +307,32 @@ __device__ __forceinline__ MrwR mrw_of(uint4 b) {
     return r;
 }
 
+template <class Pol>
+__device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl, float2 q, int s,
+                                             float uq, float urow, float ucdf, float own);
+
+// Henyey-Greenstein scattering cosine for asymmetry g from the uniform umu (isotropic
+// below |g| = 1e-4).
+__device__ __forceinline__ float hg_mu(float g, float umu) {
+    float mu;
+    if (fabsf(g) < 1.0e-4f) {
+        mu = 2.0f * umu - 1.0f;
+    } else {
+        float t = (1.0f - g * g) / (1.0f - g + 2.0f * g * umu);
+        mu = (1.0f + g * g - t * t) / (2.0f * g);
+        if (mu < -1.0f) mu = -1.0f;
+        if (mu > 1.0f) mu = 1.0f;
+    }
+    return mu;
+}
+
+// Isotropic direction from an interaction's cosine and azimuth uniforms.
+__device__ __forceinline__ void iso_of(const EvR& ev, float& kx, float& ky, float& kz) {
+    float mu = 2.0f * ev.umu - 1.0f;
+    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+    kx = st * ev.cs; ky = st * ev.sn; kz = mu;
+}
+
 // Execution policies of the transport step.
 //
 // LanePol: one packet per thread (the epoch launches and the first continuation stage).
@@ -384,6 +412,14 @@ struct LanePol {
     __device__ __forceinline__ MrwR mrwd(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
         return mrw_of(mc_block(r, n, MC_RS_MRW, k0, k1));
     }
+    __device__ __forceinline__ void iso_dir(uint32_t, const EvR& ev, float& kx, float& ky,
+                                            float& kz) const {
+        iso_of(ev, kx, ky, kz);
+    }
+    __device__ __forceinline__ float hg(uint32_t, float g, float umu) const { return hg_mu(g, umu); }
+    template <int NS>
+    __device__ __forceinline__ int reemit(const DustTabs& T, int nl, float2 q, int s, const SecR& sb,
+                                          float own, int, int, int, uint32_t);
     __device__ __forceinline__ bool cached(int, int, int, int, int) const { return false; }
     __device__ __forceinline__ void remember(int, int, int, int, int, float) {}
     // q per deposit unit of species s in cell c (wq0 = the model's [spec][cell] block)
@@ -414,6 +450,19 @@ struct WarpPol {
     EvR re;
     SecR rs;
     MrwR rm;
+    // derived per lane at the refill: the isotropic direction and, when every species has
+    // one wavelength-independent asymmetry g0 (gconst), the Henyey-Greenstein cosine
+    float ikx, iky, ikz, hgmu;
+    int gconst;
+    float g0;
+    // reemission of lane l's interaction as if it were an absorption of species 0 in cell
+    // (sk_m, sk_c) of epoch sk_e with the own deposits of when it was made (one-species
+    // walks): bucket of the row table (0 below, 1 inside, 2 above), row index j and its
+    // bounds, reemission row and wavelength bin
+    int sk_m = -1, sk_c = -1, sk_e = -1;
+    uint32_t sk_n0 = 0xffffffffu;
+    int sp_case, sp_j, sp_row, sp_lam;
+    float sp_Fj, sp_Fj1;
     // per-cell cache: (model, cell, epoch, own-deposit version) -> values by slot
     // (Rosseland, Planck per species)
     int cm, cc, ce, cv;
@@ -421,8 +470,9 @@ struct WarpPol {
     float cval[1 + MC_MAX_SPEC];
     // the packet's own-deposit cache, replicated in every lane
     McOwn own;
-    __device__ __forceinline__ explicit WarpPol(int l)
-        : lane(l), rv(false), n0(0), cm(-1), cc(-1), ce(-1), cv(-1), cvalid(0u) { own_init(own); }
+    __device__ __forceinline__ explicit WarpPol(int l, int gc, float g)
+        : lane(l), rv(false), n0(0), gconst(gc), g0(g), cm(-1), cc(-1), ce(-1), cv(-1),
+          cvalid(0u) { own_init(own); }
     __device__ __forceinline__ void own_reset() { own_init(own); }
     __device__ __forceinline__ void own_add(int sc, long long units) { ::own_add(own, sc, units); }
     __device__ __forceinline__ float own_q(int sc, float wq) const { return ::own_q(own, sc, wq); }
@@ -441,6 +491,16 @@ struct WarpPol {
     }
     // number of entries <= u of a non-decreasing table == smallest index with c > u
     __device__ __forceinline__ int cdf(const float* c, int n, float u) const {
+        if (n <= 128) {   // four independent loads, then the ballots (u < 1 < 2)
+            const float v0 = lane < n ? c[lane] : 2.0f;
+            const float v1 = 32 + lane < n ? c[32 + lane] : 2.0f;
+            const float v2 = 64 + lane < n ? c[64 + lane] : 2.0f;
+            const float v3 = 96 + lane < n ? c[96 + lane] : 2.0f;
+            return (__popc(__ballot_sync(0xffffffffu, v0 <= u)) +
+                    __popc(__ballot_sync(0xffffffffu, v1 <= u))) +
+                   (__popc(__ballot_sync(0xffffffffu, v2 <= u)) +
+                    __popc(__ballot_sync(0xffffffffu, v3 <= u)));
+        }
         int cnt = 0;
         for (int b = 0; b < n; b += 32) {
             int l = b + lane;
@@ -504,6 +564,8 @@ struct WarpPol {
             re = ev_of(mc_block(r, m, MC_RS_EVENT, k0, k1));
             rs = sec_of(mc_block(r, m, MC_RS_SECOND, k0, k1));
             rm = mrw_of(mc_block(r, m, MC_RS_MRW, k0, k1));
+            iso_of(re, ikx, iky, ikz);
+            hgmu = gconst ? hg_mu(g0, re.umu) : 0.0f;
             rv = true;
         }
         return (int)(n - n0);
@@ -535,6 +597,63 @@ struct WarpPol {
         o.jcs = __shfl_sync(0xffffffffu, rm.jcs, l);
         o.jsn = __shfl_sync(0xffffffffu, rm.jsn, l);
         return o;
+    }
+    __device__ __forceinline__ void iso_dir(uint32_t n, const EvR&, float& kx, float& ky, float& kz) const {
+        const int l = (int)(n - n0);
+        kx = __shfl_sync(0xffffffffu, ikx, l);
+        ky = __shfl_sync(0xffffffffu, iky, l);
+        kz = __shfl_sync(0xffffffffu, ikz, l);
+    }
+    __device__ __forceinline__ float hg(uint32_t n, float g, float umu) const {
+        if (gconst) return __shfl_sync(0xffffffffu, hgmu, (int)(n - n0));
+        return hg_mu(g, umu);
+    }
+    // Reemission wavelength of interaction n (an absorption of species s in cell c of model m,
+    // epoch e): the same result as reemit_lambda.  One-species walks use the lanes'
+    // speculative results, made for the whole block of 32 interactions at the first
+    // absorption in a cell: the true q' (which includes every own deposit made since) is
+    // checked against the speculative row bucket, and only the row decision is redone
+    // when it stays inside it.
+    template <int NS>
+    __device__ __forceinline__ int reemit(const DustTabs& T, int nl, float2 q, int s, const SecR& sb,
+                                          float own, int m, int c, int e, uint32_t n) {
+        if (NS > 1) return reemit_lambda(*this, T, nl, q, s, sb.uq, sb.urow, sb.ucdf, own);
+        if (m != sk_m || c != sk_c || e != sk_e || n0 != sk_n0) {
+            float qq = q.x + rs.uq * q.y;
+            qq = qq + own;
+            int j;
+            float w;
+            mc_row_search(T.F, qq, j, w);
+            sp_case = (qq < T.F[0]) ? 0 : (qq >= T.F[MC_NROW - 1]) ? 2 : 1;
+            sp_j = j;
+            sp_Fj = T.F[j];
+            sp_Fj1 = T.F[j + 1];
+            sp_row = j + ((rs.urow < w) ? 1 : 0);
+            sp_lam = mc_cdf_search(T.cdf + (size_t)sp_row * nl, nl, rs.ucdf);
+            sk_m = m; sk_c = c; sk_e = e; sk_n0 = n0;
+        }
+        const int l = (int)(n - n0);
+        const int cs_ = __shfl_sync(0xffffffffu, sp_case, l);
+        const int j = __shfl_sync(0xffffffffu, sp_j, l);
+        const int row = __shfl_sync(0xffffffffu, sp_row, l);
+        const int lam = __shfl_sync(0xffffffffu, sp_lam, l);
+        const float Fj = __shfl_sync(0xffffffffu, sp_Fj, l);
+        const float Fj1 = __shfl_sync(0xffffffffu, sp_Fj1, l);
+        float qq = q.x + sb.uq * q.y;
+        qq = qq + own;
+        if (cs_ == 0) {
+            if (qq < Fj) return lam;
+        } else if (cs_ == 2) {
+            if (qq >= Fj1) return lam;
+        } else if (Fj <= qq && qq < Fj1) {
+            float w = (qq - Fj) / (Fj1 - Fj);
+            if (w < 0.0f) w = 0.0f;
+            if (w > 1.0f) w = 1.0f;
+            const int rt = j + ((sb.urow < w) ? 1 : 0);
+            if (rt == row) return lam;
+            return cdf(T.cdf + (size_t)rt * nl, nl, sb.ucdf);
+        }
+        return reemit_lambda(*this, T, nl, q, s, sb.uq, sb.urow, sb.ucdf, own);
     }
     __device__ __forceinline__ bool cached(int m, int c, int e, int v, int k) const {
         return cm == m && cc == c && ce == e && cv == v && ((cvalid >> k) & 1u);
@@ -616,6 +735,12 @@ __device__ __forceinline__ int reemit_lambda(Pol& pol, const DustTabs& T, int nl
     pol.row(T.F + s * MC_NROW, qq, j, w);
     int row = j + ((urow < w) ? 1 : 0);
     return pol.cdf(T.cdf + ((size_t)s * MC_NROW + row) * nl, nl, ucdf);
+}
+
+template <int NS>
+__device__ __forceinline__ int LanePol::reemit(const DustTabs& T, int nl, float2 q, int s,
+                                               const SecR& sb, float own, int, int, int, uint32_t) {
+    return reemit_lambda(*this, T, nl, q, s, sb.uq, sb.urow, sb.ucdf, own);
 }
 
 template <class G>
@@ -851,17 +976,7 @@ __device__ __forceinline__ bool mc_step(typename G::Pkt& p, const McParams& P, c
                         if (us < acc) { sp = s; break; }
                     }
                 }
-                float g = T.g[sp * nl + p.lam];
-                float umu = ev.umu;
-                float mu;
-                if (fabsf(g) < 1.0e-4f) {
-                    mu = 2.0f * umu - 1.0f;
-                } else {
-                    float t = (1.0f - g * g) / (1.0f - g + 2.0f * g * umu);
-                    mu = (1.0f + g * g - t * t) / (2.0f * g);
-                    if (mu < -1.0f) mu = -1.0f;
-                    if (mu > 1.0f) mu = 1.0f;
-                }
+                const float mu = pol.hg(n, T.g[sp * nl + p.lam], ev.umu);
                 mc_rotate(p.kx, p.ky, p.kz, mu, ev.cs, ev.sn);
                 cnt.scatter += 1;
             } else {
@@ -884,13 +999,11 @@ __device__ __forceinline__ bool mc_step(typename G::Pkt& p, const McParams& P, c
                 if (pol.leader()) atomicAdd((unsigned long long*)(dep + idx), 1ull << MC_EUNIT_SHIFT);
                 pol.own_add(sp * M.ncell + c, 1ll << MC_EUNIT_SHIFT);
                 const float2 qs = pol.template snap<NS>(qa + base, M.ncell, p.m, c, p.epoch, sp);
-                p.lam = reemit_lambda(pol, T, nl, qs, sp, sb.uq, sb.urow, sb.ucdf,
-                                      pol.own_q(sp * M.ncell + c, pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, sp)));
-                {
-                    float mu = 2.0f * ev.umu - 1.0f;
-                    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
-                    p.kx = st * ev.cs; p.ky = st * ev.sn; p.kz = mu;
-                }
+                p.lam = pol.template reemit<NS>(
+                    T, nl, qs, sp, sb,
+                    pol.own_q(sp * M.ncell + c, pol.template wq<NS>(P.wq + base, M.ncell, p.m, c, sp)),
+                    p.m, c, p.epoch, n);
+                pol.iso_dir(n, ev, p.kx, p.ky, p.kz);
                 cnt.absorb += 1;
             }
             p.tau = ev.tn;
@@ -1154,6 +1267,157 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
     }
 }
 
+// Fast path of the warp-per-packet walk for one dust species and the double-single
+// geometry: interactions inside the packet's current cell that need no wall solve, written
+// out with the cell's density, snapshot, q per deposit unit and walls held in registers.
+// It covers the steps of a trapped packet: the safety-distance refresh, an MRW try and the
+// MRW jump itself.  A step that needs anything else (a wall solve, a crossing, a value not
+// cached yet, the interaction cap) is left to mc_step before anything of it is committed,
+// and mc_step then takes exactly the decisions the fast path would have taken: the result
+// is identical either way.
+struct TailCell {
+    int ir = -2, itv = -1, ip = -1, epoch = -1;
+    int c;
+    float rho, wq;
+    float2 q;
+};
+
+// Runs fast steps of packet p until one does not qualify (returns 0: the caller runs
+// mc_step next) or the budget of steps is spent (1).  steps counts the steps taken.
+__device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const McModel& M,
+                                             const DustTabs& T, Cnt& cnt, WarpPol& pol,
+                                             TailCell& tc, int budget, int& steps) {
+    const int nl = P.nl;
+    const uint32_t k0 = P.key0, k1 = P.key1;
+    const int64_t base = M.cell_off;
+    const int lane = pol.lane;
+    for (steps = 0; steps < budget; ++steps) {
+        if (p.ir < 0) return 0;
+        if (p.ir != tc.ir || p.itv != tc.itv || p.ip != tc.ip || p.epoch != tc.epoch) {
+            tc.c = cell_of_s(M, p);
+            tc.ir = p.ir; tc.itv = p.itv; tc.ip = p.ip; tc.epoch = p.epoch;
+            tc.rho = __ldg(P.rho + base + tc.c);
+            tc.wq = __ldg(P.wq + base + tc.c);
+            tc.q = P.q[(int64_t)p.epoch * P.qstride + base + tc.c];
+        }
+        const int c = tc.c;
+        const float rh = tc.rho;
+        float alpha = 0.0f;
+        alpha = alpha + rh * T.kext[p.lam];
+        if (!(alpha > 0.0f)) return 0;
+        const float sef = p.tau / alpha;
+        if (!(sef < p.dsafe) && !p.fresh) {
+            const float D = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+            p.dsafe = 0.999999f * D;
+            p.dmax = mc_dmax_of(D);
+            p.fresh = 1;
+        }
+        if (!(sef < p.dsafe)) return 0;                 // a wall solve is due
+        // everything mc_step decides before committing: the MRW try and the cap
+        const float dmax1 = mc_dmax_after(p.dmax, sef);
+        const int nev1 = p.nevents + 1;
+        const int cev1 = p.cell_events + 1;
+        if (nev1 >= P.max_inter) return 0;
+        const bool cond = P.mrw && (cev1 >= P.mrw_trigger ||
+                                    (P.mrw_eager_after > 0 && nev1 > P.mrw_eager_after));
+        bool tried = false;
+        float aR = 0.0f;
+        if (cond && 0.999f * dmax1 * alpha >= P.mrw_tauthres) {
+            if (!pol.cached(p.m, c, p.epoch, pol.own_ver(), 0)) return 0;
+            aR = pol.cached_value(0);
+            tried = 0.999f * dmax1 * aR >= P.mrw_gamma;
+        }
+        if (tried && !pol.cached(p.m, c, p.epoch, pol.own_ver(), 1)) return 0;
+        // the interaction
+        p.x = ds_move(p.x, sef, p.kx);
+        p.y = ds_move(p.y, sef, p.ky);
+        p.z = ds_move(p.z, sef, p.kz);
+        p.dsafe = p.dsafe - sef;
+        p.fresh = 0;
+        p.last_wall = W_NONE;
+        const uint32_t n = (uint32_t)p.nevents;
+        p.cell_events = cev1;
+        p.nevents = nev1;
+        cnt.events += 1;
+        const bool late = P.late_after > 0 && nev1 > P.late_after;
+        int64_t* dep = late ? P.Elate : P.E;
+        const EvR ev = pol.ev(p.rng, n, k0, k1);
+        p.dmax = dmax1;
+        bool did_mrw = false;
+        float Dw = 0.0f;
+        if (tried) {
+            Dw = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+            const float R0f = 0.999f * Dw;
+            if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
+                did_mrw = true;
+                const MrwR mb = pol.mrwd(p.rng, n, k0, k1);
+                const SecR sb = pol.second(p.rng, n, k0, k1);
+                float f = mb.uy * (float)(MC_NMRW - 1);
+                int i = (int)f;
+                if (i > MC_NMRW - 2) i = MC_NMRW - 2;
+                float w = f - (float)i;
+                float yv = T.mrw[i] + w * (T.mrw[i + 1] - T.mrw[i]);
+                float ell = 3.0f * aR * R0f * R0f * yv;
+                const float kp = pol.cached_value(1);
+                float units_f = kp * ell * 1048576.0f + 0.5f;
+                if (units_f > 9.0e18f) units_f = 9.0e18f;
+                long long units = (long long)units_f;
+                if (units > 0) {
+                    if (lane == 0)
+                        atomicAdd((unsigned long long*)(dep + base + c), (unsigned long long)units);
+                    pol.own_add(c, units);
+                }
+                float dx, dy, dz;
+                {
+                    float mu = mb.jmu;
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+                    dx = st * mb.jcs; dy = st * mb.jsn; dz = mu;
+                }
+                p.x = ds_move(p.x, R0f, dx);
+                p.y = ds_move(p.y, R0f, dy);
+                p.z = ds_move(p.z, R0f, dz);
+                {
+                    float mu = sqrtf(ev.umu);
+                    float kx = dx, ky = dy, kz = dz;
+                    mc_rotate(kx, ky, kz, mu, ev.cs, ev.sn);
+                    p.kx = kx; p.ky = ky; p.kz = kz;
+                }
+                p.lam = reemit_lambda(pol, T, nl, tc.q, 0, sb.uq, sb.urow, sb.ucdf,
+                                      pol.own_q(c, tc.wq));
+                p.tau = ev.tn;
+                p.cell_events = 0;
+                cnt.mrw += 1;
+            }
+        }
+        if (!did_mrw) {
+            float asca = 0.0f;
+            asca = asca + rh * T.ksca[p.lam];
+            if (ev.ua * alpha < asca) {
+                const float mu = pol.hg(n, T.g[p.lam], ev.umu);
+                mc_rotate(p.kx, p.ky, p.kz, mu, ev.cs, ev.sn);
+                cnt.scatter += 1;
+            } else {
+                const SecR sb = pol.second(p.rng, n, k0, k1);
+                if (lane == 0) atomicAdd((unsigned long long*)(dep + base + c), 1ull << MC_EUNIT_SHIFT);
+                pol.own_add(c, 1ll << MC_EUNIT_SHIFT);
+                p.lam = pol.template reemit<1>(T, nl, tc.q, 0, sb, pol.own_q(c, tc.wq), p.m, c,
+                                               p.epoch, n);
+                pol.iso_dir(n, ev, p.kx, p.ky, p.kz);
+                cnt.absorb += 1;
+            }
+            p.tau = ev.tn;
+        }
+        if (did_mrw) Dw = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+        if (did_mrw || tried) {
+            p.dsafe = 0.999999f * Dw;
+            p.dmax = mc_dmax_of(Dw);
+            p.fresh = 1;
+        }
+        if (late) cnt.late += 1;
+    }
+    return 1;
+}
+
 // Continuation of parked packets: one packet per warp (WarpPol), taken from a queue.
 template <int NS, class G>
 __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
@@ -1190,15 +1454,26 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         g = __shfl_sync(0xffffffffu, g, 0);
         if ((long long)g >= total) break;
         typename G::Pkt p;
-        WarpPol pol(lane);
+        WarpPol pol(lane, P.g_const, P.g0);
         park_load<G>(p, P.park_in[g], pol);
         // the packet's model, held in registers for the whole walk
         const McModel Mw = P.models[p.m];
         int live = 1;
         if (lane == 0) live = model_live(P, p.m) ? 1 : 0;
         bool alive = __shfl_sync(0xffffffffu, live, 0) != 0;
+        TailCell tc;
         while (alive) {
-            alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
+            if constexpr (NS == 1 && std::is_same<G, GeoS>::value) {
+                // fast steps up to the next periodic check, then one general step
+                int nfast = 0;
+                const int r = tail_fast_run(p, P, Mw, T, cnt, pol, tc, 4096 - (int)(iter & 4095u),
+                                            nfast);
+                iter += (unsigned)nfast;
+                if (r == 0) alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
+                else iter -= 1u;   // the budget ran out: the check below comes next
+            } else {
+                alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
+            }
             if (((++iter) & 4095u) == 0u) {
                 int st = 0;
                 if (lane == 0) {
@@ -1366,6 +1641,8 @@ struct pdgpu_mc_plan {
         ws_queue, ws_total, tables_bytes, ws_Elate, ws_park, ws_park2, ws_parkcnt, ws_wq,
         ws_mdl, ws_mstat;
     bool use_mdl;                   // per-model deadlines set (pdgpu_mc_plan_set_model_deadlines)
+    bool g_const;                   // one wavelength-independent asymmetry g0 for every species
+    float g0;
     int64_t park_cap;
     int nqueue;
     int device, nsm, block, grid;
@@ -1490,6 +1767,10 @@ pdgpu_status build_dust(pdgpu_mc_plan* P, const pdgpu_dust_desc* d, std::vector<
     const std::vector<float>& mt = mrw_table();
     for (int i = 0; i < MC_NMRW; ++i) f[P->o_mrw + i] = mt[i];
     P->dust_floats = (int)f.size();
+    P->g_const = true;
+    P->g0 = f[P->o_g];
+    for (int i = 1; i < ns * nl; ++i)
+        if (f[P->o_g + i] != P->g0) P->g_const = false;
     // pad to 16 bytes so the stellar CDFs start aligned
     while (f.size() % 4) f.push_back(0.0f);
     return PDGPU_OK;
@@ -1864,6 +2145,8 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.o_F = P->o_F; prm.o_cdf = P->o_cdf; prm.o_kP = P->o_kP; prm.o_kR = P->o_kR;
     prm.o_mrw = P->o_mrw;
     prm.count_stats = final_pass ? 1 : 0;
+    prm.g_const = P->g_const ? 1 : 0;
+    prm.g0 = P->g0;
     if (prm.total <= 0) return PDGPU_OK;
     void (*kern)(McParams) = nullptr;
     const bool f64 = P->opt.fp64_walls != 0;
