@@ -358,6 +358,34 @@ __device__ inline ds next_wall_ds(const McModel& M, const Wl& W, const PktS& p,
     return refine_ds(M, W, p, f, bk, best);
 }
 
+// The same wall solve for a packet inside the grid (ir >= 0) with a compile-time candidate
+// count (4 without phi walls, 6 with): the candidates are independent, so unrolled they
+// are evaluated side by side; the selection is the same (first smallest distance).
+template <int NK, class Wl>
+__device__ __forceinline__ ds next_wall_ds_n(const McModel& M, const Wl& W, const PktS& p,
+                                             int& wall_out) {
+    FrameS f;
+    frame_ds(M, W, p, f);
+    float sk[NK];
+    bool ok[NK];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) ok[k] = candidate_ds(M, W, p, f, k, sk[k]);
+    float best = 3.0e38f;
+    int bk = -1;
+#pragma unroll
+    for (int k = 0; k < NK; ++k)
+        if (ok[k] && sk[k] < best) {
+            best = sk[k];
+            bk = k;
+        }
+    if (bk < 0) {
+        wall_out = W_NONE;
+        return ds{3.0e38f, 0.0f};
+    }
+    wall_out = cand_wall_code(bk);
+    return refine_ds(M, W, p, f, bk, best);
+}
+
 // Virtual theta wall j lies at or below the packet's polar angle (cos theta_j >= z / r),
 // decided from the sign of z^2 - mu_j^2 r^2 in double-single.
 template <class Wl>

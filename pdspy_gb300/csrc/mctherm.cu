@@ -1268,13 +1268,14 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
 }
 
 // Fast path of the warp-per-packet walk for one dust species and the double-single
-// geometry: interactions inside the packet's current cell that need no wall solve, written
-// out with the cell's density, snapshot, q per deposit unit and walls held in registers.
-// It covers the steps of a trapped packet: the safety-distance refresh, an MRW try and the
-// MRW jump itself.  A step that needs anything else (a wall solve, a crossing, a value not
-// cached yet, the interaction cap) is left to mc_step before anything of it is committed,
-// and mc_step then takes exactly the decisions the fast path would have taken: the result
-// is identical either way.
+// geometry, written for the latency of one dependent chain: the cell's density, snapshot,
+// q per deposit unit and walls are held in registers, every lane evaluates the geometry
+// itself (straight-line code, no shuffles), and the random numbers, isotropic directions,
+// scattering cosines and reemission wavelengths come from the lanes' precomputed values.
+// It takes the same decisions in the same order as mc_step (safety-distance refresh, wall
+// solve, interaction or crossing, MRW try and jump), so the result is identical; the rare
+// cases (a packet inside the inner hole, an empty cell, the interaction cap) are left to
+// mc_step before anything of the step is committed.
 struct TailCell {
     int ir = -2, itv = -1, ip = -1, epoch = -1;
     int c;
@@ -1282,8 +1283,13 @@ struct TailCell {
     float2 q;
 };
 
-// Runs fast steps of packet p until one does not qualify (returns 0: the caller runs
-// mc_step next) or the budget of steps is spent (1).  steps counts the steps taken.
+__device__ __forceinline__ ds tail_wall(const McModel& M, const WallsCell& W, const PktS& p,
+                                        int& wall) {
+    return M.np > 1 ? next_wall_ds_n<6>(M, W, p, wall) : next_wall_ds_n<4>(M, W, p, wall);
+}
+
+// Runs steps of packet p until one must go to mc_step (returns 0), the budget of steps is
+// spent (1) or the packet has left the grid or was killed (2).  steps counts the steps taken.
 __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const McModel& M,
                                              const DustTabs& T, Cnt& cnt, WarpPol& pol,
                                              TailCell& tc, int budget, int& steps) {
@@ -1300,53 +1306,99 @@ __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const M
             tc.wq = __ldg(P.wq + base + tc.c);
             tc.q = P.q[(int64_t)p.epoch * P.qstride + base + tc.c];
         }
+        const WallsCell& W = pol.cell_walls(M, P.fpool, p);
         const int c = tc.c;
         const float rh = tc.rho;
         float alpha = 0.0f;
         alpha = alpha + rh * T.kext[p.lam];
         if (!(alpha > 0.0f)) return 0;
+        if (p.nevents + 1 >= P.max_inter) return 0;
         const float sef = p.tau / alpha;
         if (!(sef < p.dsafe) && !p.fresh) {
-            const float D = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+            const float D = wall_distance_ds(M, W, p);
             p.dsafe = 0.999999f * D;
             p.dmax = mc_dmax_of(D);
             p.fresh = 1;
         }
-        if (!(sef < p.dsafe)) return 0;                 // a wall solve is due
-        // everything mc_step decides before committing: the MRW try and the cap
-        const float dmax1 = mc_dmax_after(p.dmax, sef);
-        const int nev1 = p.nevents + 1;
-        const int cev1 = p.cell_events + 1;
-        if (nev1 >= P.max_inter) return 0;
-        const bool cond = P.mrw && (cev1 >= P.mrw_trigger ||
-                                    (P.mrw_eager_after > 0 && nev1 > P.mrw_eager_after));
-        bool tried = false;
-        float aR = 0.0f;
-        if (cond && 0.999f * dmax1 * alpha >= P.mrw_tauthres) {
-            if (!pol.cached(p.m, c, p.epoch, pol.own_ver(), 0)) return 0;
-            aR = pol.cached_value(0);
-            tried = 0.999f * dmax1 * aR >= P.mrw_gamma;
+        const bool full = !(sef < p.dsafe);
+        ds se = ds{sef, 0.0f};
+        if (full) {
+            int wall = W_NONE;
+            const ds sw = tail_wall(M, W, p, wall);
+            const float tcell = alpha * sw.h;
+            if (!(tcell > p.tau)) {
+                // crossing into the next cell
+                p.x = ds_move2(p.x, sw, p.kx);
+                p.y = ds_move2(p.y, sw, p.ky);
+                p.z = ds_move2(p.z, sw, p.kz);
+                p.tau = p.tau - tcell;
+                p.dsafe = 0.0f;
+                p.dmax = MC_DMAX_UNKNOWN;
+                p.fresh = 1;
+                p.ncross += 1;
+                cnt.crossings += 1;
+                p.cell_events = 0;
+                switch (wall) {
+                    case W_ROUT:
+                        p.ir += 1;
+                        p.last_wall = W_RIN;
+                        if (p.ir >= M.nr) {
+                            cnt.escaped += 1;
+                            if (P.escape && lane == 0)
+                                atomicAdd((unsigned long long*)(P.escape + (int64_t)p.m * nl + p.lam), 1ull);
+                            return 2;
+                        }
+                        break;
+                    case W_RIN: p.ir -= 1; p.last_wall = W_ROUT; break;
+                    case W_TLO: p.itv -= 1; p.last_wall = W_THI; break;
+                    case W_THI: p.itv += 1; p.last_wall = W_TLO; break;
+                    case W_PLO: p.ip = (p.ip == 0) ? M.np - 1 : p.ip - 1; p.last_wall = W_PHI; break;
+                    case W_PHI: p.ip = (p.ip == M.np - 1) ? 0 : p.ip + 1; p.last_wall = W_PLO; break;
+                    default: cnt.killed += 1; return 2;
+                }
+                if (p.ncross > 100000000) {
+                    cnt.killed += 1;
+                    return 2;
+                }
+                continue;
+            }
+            se = ds{p.tau / alpha, 0.0f};
+            if (se.h > sw.h) se = sw;
         }
-        if (tried && !pol.cached(p.m, c, p.epoch, pol.own_ver(), 1)) return 0;
         // the interaction
-        p.x = ds_move(p.x, sef, p.kx);
-        p.y = ds_move(p.y, sef, p.ky);
-        p.z = ds_move(p.z, sef, p.kz);
-        p.dsafe = p.dsafe - sef;
+        p.x = ds_move2(p.x, se, p.kx);
+        p.y = ds_move2(p.y, se, p.ky);
+        p.z = ds_move2(p.z, se, p.kz);
+        p.dsafe = full ? 0.0f : p.dsafe - sef;
         p.fresh = 0;
         p.last_wall = W_NONE;
         const uint32_t n = (uint32_t)p.nevents;
-        p.cell_events = cev1;
-        p.nevents = nev1;
+        p.cell_events += 1;
+        p.nevents += 1;
         cnt.events += 1;
-        const bool late = P.late_after > 0 && nev1 > P.late_after;
+        const bool late = P.late_after > 0 && p.nevents > P.late_after;
         int64_t* dep = late ? P.Elate : P.E;
         const EvR ev = pol.ev(p.rng, n, k0, k1);
-        p.dmax = dmax1;
+        p.dmax = mc_dmax_after(p.dmax, se.h);
         bool did_mrw = false;
+        const bool cond = P.mrw && (p.cell_events >= P.mrw_trigger ||
+                                    (P.mrw_eager_after > 0 && p.nevents > P.mrw_eager_after));
+        bool tried = false;
         float Dw = 0.0f;
+        float aR = 0.0f;
+        if (cond && 0.999f * p.dmax * alpha >= P.mrw_tauthres) {
+            if (pol.cached(p.m, c, p.epoch, pol.own_ver(), 0)) {
+                aR = pol.cached_value(0);
+            } else {
+                float qm = tc.q.x + 0.5f * tc.q.y;
+                qm = qm + pol.own_q(c, tc.wq);
+                aR = aR + rh * row_interp(pol, T, T.kR, qm, 0);
+                pol.remember(p.m, c, p.epoch, pol.own_ver(), 0, aR);
+            }
+            tried = 0.999f * p.dmax * aR >= P.mrw_gamma;
+        }
         if (tried) {
-            Dw = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+            Dw = wall_distance_ds(M, W, p);
             const float R0f = 0.999f * Dw;
             if (R0f * aR >= P.mrw_gamma && R0f * alpha >= P.mrw_tauthres) {
                 did_mrw = true;
@@ -1358,7 +1410,15 @@ __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const M
                 float w = f - (float)i;
                 float yv = T.mrw[i] + w * (T.mrw[i + 1] - T.mrw[i]);
                 float ell = 3.0f * aR * R0f * R0f * yv;
-                const float kp = pol.cached_value(1);
+                float kp;
+                if (pol.cached(p.m, c, p.epoch, pol.own_ver(), 1)) {
+                    kp = pol.cached_value(1);
+                } else {
+                    float qm = tc.q.x + 0.5f * tc.q.y;
+                    qm = qm + pol.own_q(c, tc.wq);
+                    kp = rh * row_interp(pol, T, T.kP, qm, 0);
+                    pol.remember(p.m, c, p.epoch, pol.own_ver(), 1, kp);
+                }
                 float units_f = kp * ell * 1048576.0f + 0.5f;
                 if (units_f > 9.0e18f) units_f = 9.0e18f;
                 long long units = (long long)units_f;
@@ -1407,7 +1467,7 @@ __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const M
             }
             p.tau = ev.tn;
         }
-        if (did_mrw) Dw = wall_distance_ds_warp(M, pol.cell_walls(M, P.fpool, p), p, lane);
+        if (did_mrw) Dw = wall_distance_ds(M, W, p);
         if (did_mrw || tried) {
             p.dsafe = 0.999999f * Dw;
             p.dmax = mc_dmax_of(Dw);
@@ -1470,6 +1530,7 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
                                             nfast);
                 iter += (unsigned)nfast;
                 if (r == 0) alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
+                else if (r == 2) alive = false;
                 else iter -= 1u;   // the budget ran out: the check below comes next
             } else {
                 alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
