@@ -12,12 +12,15 @@ A step is one full thermal run of the batch (all epochs, both continuation stage
 temperature inversion).  ``value`` is packets/s with the densities resident in HBM (CUDA
 events around the run); ``e2e`` is the same step through the public API with host arrays,
 timed on the same stream from the pinned H2D copy of the densities to the D2H copy of the
-temperatures.  The longest packet walk of this workload (3e7 interactions for one walker
-at 1e6 packets with the default seed; the walk lengths are heavy-tailed) sets most of a
-step's time, so the default is one timed step and warm-up runs are cut at a short device
-deadline.  The reference arm (``--impl reference``) times the CPU restatement of the same
-algorithm (the reference's own path is the external RADMC-3D binary, which is not
-available) on a bounded sample of the workload: every walker at 2e4 packets.
+temperatures.  The longest packet walks of this workload (about 1.5e8 interactions for one
+walker at 1e6 packets with the default seed; the walk lengths are heavy-tailed, as in
+sequential Bjorkman & Wood) set most of a step's time, so step k runs Monte Carlo seed
+seed + k and the line reports every step's time with its tail (the warp-per-packet stage)
+and bulk parts; warm-up runs are cut at a short device deadline.  The reference arm
+(``--impl reference``) times the CPU restatement of the same algorithm (the reference's
+own path is the external RADMC-3D binary, which is not available) on a bounded sample of
+the workload, every walker at 1e4 packets in a pool of single-threaded workers
+(``--cpu-full``: the whole workload).
 
 The same JSON line carries the adjoint gradient rate, the scattering source of an SED
 (with its CPU restatement), gridded vs direct visibility sampling and, with
@@ -67,7 +70,9 @@ def parse():
                     help="also time the batched MCMC lnprob of this many walkers (0: off)")
     ap.add_argument("--lnprob-packets", type=int, default=100000)
     ap.add_argument("--cpu-models", type=int, default=64)
-    ap.add_argument("--cpu-packets", type=int, default=20000)
+    ap.add_argument("--cpu-packets", type=int, default=10000)
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="reference arm: run the whole workload (every model at --packets)")
     ap.add_argument("--timelimit", type=float, default=1800.0,
                     help="device-side deadline per timed thermal run (s)")
     ap.add_argument("--warmup-deadline", type=float, default=10.0,
@@ -131,6 +136,34 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
+def l2_roofs(dev):
+    """Measured L2 roofs on this GPU: an L2-resident copy (two 24 MB buffers, read + write
+    bytes) and int64 atomic adds into a 32 MB array (torch.index_add_), best of 5."""
+    import torch
+    n = (24 << 20) // 4
+    a = torch.ones(n, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    acc = torch.zeros(4 << 20, dtype=torch.int64, device=dev)
+    m = 16 << 20
+    idx = torch.randint(0, acc.numel(), (m,), device=dev)
+    one = torch.ones(m, dtype=torch.int64, device=dev)
+    best_c, best_a = 0.0, 0.0
+    for _ in range(5):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        for _ in range(20):
+            b.copy_(a)
+        e[1].record()
+        acc.index_add_(0, idx, one)
+        e[2].record()
+        torch.cuda.synchronize(dev)
+        best_c = max(best_c, 20 * 2 * 4 * n / (e[0].elapsed_time(e[1]) / 1e3) / 1e9)
+        best_a = max(best_a, m / (e[1].elapsed_time(e[2]) / 1e3))
+    return {"copy_gbs": best_c, "red_per_s": best_a,
+            "how": "L2-resident torch copy of 24 MB (read + write bytes) and torch.index_add_ of "
+                   "16M int64 ones into 4M cells, best of 5, this run"}
+
+
 def cpu_model():
     """Host CPU model string and thread count (lscpu's model name, else platform)."""
     import platform
@@ -181,21 +214,36 @@ def build_models(args, rank):
     return workloads.walker_models(n=args.models, seed=args.seed + 1000 * rank)
 
 
-def cpu_sample(models, args, threads):
-    """The CPU restatement on the first cpu-models walkers (all of them by default, so the
-    sample has the workload's mix of light and heavy walkers) at cpu-packets packets each, in
-    its FP64-geometry build (native double precision is the fast choice on host cores)."""
-    from oracle import orc  # noqa: F401  (CPU baseline leg only)
-    from tests import _cases
+def _cpu_walker(job):
+    """One model of the workload through the CPU restatement, single-threaded (a worker of
+    cpu_sample's process pool): returns (packets, events, longest walk)."""
+    wl, nmodels, wseed, i, nphot, seed = job
+    from tests import _cases  # CPU baseline leg only
+    ns = argparse.Namespace(workload=wl, models=nmodels, seed=wseed)
+    m = build_models(ns, 0)[i]
+    r = _cases.run_oracle(m, nphot, seed=seed, model_id=i, nthreads=1, fp64_walls=True, **MRW)
+    return nphot, r["stats"]["events"], r["stats"]["max_packet_events"]
+
+
+def cpu_sample(models, args, threads, seed=None, packets=None, nmodels=None):
+    """The CPU restatement (FP64-geometry build: native double precision is the fast choice
+    on host cores) on the first nmodels models of the workload (all of them by default, so
+    the sample has the workload's mix of light and heavy walkers) at ``packets`` packets
+    each.  The models run in a spawn-started pool of ``threads`` single-threaded workers,
+    the way pdspy's MPI pool spreads walkers over cores; a long walk occupies one core while
+    the others go on.  Returns (packets/s, seconds, interactions, longest walk)."""
+    import multiprocessing as mp
+    seed = args.seed if seed is None else seed
+    packets = args.cpu_packets if packets is None else packets
+    nm = min(args.cpu_models if nmodels is None else nmodels, len(models))
+    jobs = [(args.workload, args.models, args.seed, i, packets, seed) for i in range(nm)]
+    jobs.sort(key=lambda j: -models[j[3]].grid.density[0].size)   # big grids first
     t0 = time.time()
-    pk = 0
-    nm = min(args.cpu_models, len(models))
-    for i, m in enumerate(models[:nm]):
-        _cases.run_oracle(m, args.cpu_packets, seed=args.seed, model_id=i, nthreads=threads,
-                          fp64_walls=True, **MRW)
-        pk += args.cpu_packets
+    with mp.get_context("spawn").Pool(max(1, min(threads, nm))) as pool:
+        res = pool.map(_cpu_walker, jobs, chunksize=1)
     dt = time.time() - t0
-    return pk / dt, dt
+    pk = sum(r[0] for r in res)
+    return pk / dt, dt, int(sum(r[1] for r in res)), int(max(r[2] for r in res))
 
 
 def adjoint_rate(dev, seed, reps):
@@ -387,17 +435,25 @@ def run_reference(args, world, rank):
         return
     threads = os.cpu_count()
     models = build_models(args, 0)
+    # warm-up: page the library and the interpreter in on a small sample (one model)
     for _ in range(args.warmup):
-        cpu_sample(models, args, threads)
-    vals, times = [], []
-    for _ in range(args.steps):
-        v, dt = cpu_sample(models, args, threads)
-        vals.append(v)
+        cpu_sample(models, args, threads, packets=2000, nmodels=1)
+    full = args.cpu_full
+    packets = args.packets if full else args.cpu_packets
+    nm = len(models) if full else min(args.cpu_models, len(models))
+    times, events, longest = [], [], []
+    for k in range(args.steps):
+        # step k uses Monte Carlo seed seed + k, as the GPU arm's step k does
+        v, dt, ev, lw = cpu_sample(models, args, threads, seed=args.seed + k, packets=packets,
+                                   nmodels=nm)
         times.append(dt)
-    nm = min(args.cpu_models, len(models))
-    value = float(nm * args.cpu_packets * args.steps / np.sum(times))
-    sample = "%d models x %d packets (of the %d x %g workload), CPU restatement (FP64 geometry), %d threads" % (
-        nm, args.cpu_packets, args.models, args.packets, threads)
+        events.append(ev)
+        longest.append(lw)
+    value = float(nm * packets * args.steps / np.sum(times))
+    sample = ("%d models x %d packets (%s the %d x %g workload), CPU restatement (FP64 "
+              "geometry), %d single-threaded workers" % (nm, packets, "all of" if full else
+                                                          "a sample of", args.models,
+                                                          args.packets, threads))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "packets/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(times) * 1e3), "higher_is_better": True,
@@ -406,7 +462,12 @@ def run_reference(args, world, rank):
             "cpu_baseline": {"value": value, "unit": "packets/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "packets/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "interactions": {"per_s": float(np.sum(events) / np.sum(times)),
+                             "longest_walk": longest},
+            "seeds": {"mc_seeds": [args.seed + k for k in range(args.steps)],
+                      "ms_per_step": [round(t * 1e3, 1) for t in times]},
+            "host_cpu": cpu_model()}
     print(json.dumps(line), flush=True)
 
 
@@ -457,6 +518,7 @@ def main():
     # densities, event b, the thermal run, event c, device -> pinned host copy of the
     # temperatures, event d.  value uses b..c (inputs resident in HBM), e2e uses a..d.
     step_ms, e2e_ms, launch_ms, launch_stats, stats = [], [], [], [], []
+    launch_counts = []
     with Clocks(local) as clk:
         for k in range(args.steps):
             plan = plans[k]
@@ -475,6 +537,7 @@ def main():
             e2e_ms.append(ev[0].elapsed_time(ev[3]))
             launch_ms.append(plan.launch_ms())
             launch_stats.append(plan.launch_stats())
+            launch_counts.append(plan.launch_counts())
             stats.append(plan.check_status())
 
     # per step: the warp-per-packet stage (the last transport launch: the longest walks) and
@@ -517,7 +580,6 @@ def main():
             traffic = json.load(open(tf)).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    achieved = (alg_bytes / n_launch) / (avg_launch / 1e3) / 1e9
     events_all = float(np.sum([st_["events"] for st_ in stats]))
     t_bulk = max_over_ranks(float(np.sum(bulk_ms)), world, dev)
     interactions = {"per_s": world * events_all / (t_max / 1e3),
@@ -525,15 +587,47 @@ def main():
                     "note": "interactions (absorptions, scatterings, MRW steps) per second over the "
                             "timed steps; bulk_per_s divides by the time before the "
                             "warp-per-packet stage"}
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "kernel": "mc_transport_kernel + mc_continue_kernel (every walk launch)",
+    # per launch of the last step: algorithmic bytes = 4 nspec B per crossing (densities)
+    # + 8 B per deposit (int64 atomic) + 4 B per reemission (temperature snapshot)
+    lc = launch_counts[-1]
+
+    def alg(d):
+        return 4 * ns * d["crossings"] + 12 * d["deposits"]
+
+    tail = lc[-1] if lc else None
+    bulk = lc[:-1]
+    t_bulk_k = sum(d["ms"] for d in bulk) / 1e3
+    dominant = max(lc, key=lambda d: d["ms"]) if lc else None
+    sm_mhz = 2070.0
+    roofline = {"bound": "hbm", "peak": peak, "unit": "GB/s",
                 "peak_source": "measured" if peaks else "fallback",
-                "traffic_source": "null: ncu DRAM bytes per walk launch are 0.26-0.35 MB on the "
-                                  "plain disk (profiles/), the working set stays in L2",
+                "kernel": "mc_continue_kernel (the warp-per-packet stage: the longest walks, "
+                          "%.0f%% of the last step)" % (100 * tail["ms"] / step_ms[-1])
+                          if tail and dominant is tail else "mc_transport_kernel",
+                "traffic": traffic,
+                "traffic_source": "null: the walk kernels' working set (densities, snapshots, "
+                                  "deposits) stays in L2; profiles/ holds the ncu DRAM bytes",
                 "launches_per_step": n_launch,
                 "walk_kernel_ms_last_step": float(np.sum(lm)),
-                "algorithmic_bytes_last_step": int(alg_bytes)}
+                "algorithmic_bytes_last_step": int(sum(alg(d) for d in lc))}
+    if dominant is not None:
+        a_dom = alg(dominant) / (dominant["ms"] / 1e3) / 1e9
+        roofline.update(achieved=a_dom, frac=a_dom / peak)
+        if dominant["events"] > 0:
+            roofline["cycles_per_interaction"] = dominant["ms"] * 1e-3 * sm_mhz * 1e6 / dominant["events"]
+            roofline["latency_note"] = ("a single dependent chain per packet: the bound is the "
+                                        "latency of one interaction, not a memory or issue roof")
+    l2 = l2_roofs(dev) if rank == 0 else None
+    if l2 and t_bulk_k > 0:
+        ab = sum(alg(d) for d in bulk) / t_bulk_k / 1e9
+        at = sum(d["deposits"] for d in bulk) / t_bulk_k
+        roofline["bulk"] = {"kernel": "mc_transport_kernel (epoch and first continuation launches)",
+                            "l2_achieved_gbs": ab, "l2_peak_gbs": l2["copy_gbs"],
+                            "l2_frac": ab / l2["copy_gbs"], "atomics_per_s": at,
+                            "atomic_peak_per_s": l2["red_per_s"],
+                            "atomic_frac": at / l2["red_per_s"],
+                            "interactions_per_s": sum(d["events"] for d in bulk) / t_bulk_k,
+                            "peaks_source": l2["how"]}
 
     adj = None
     if rank == 0 and not args.no_adjoint:
@@ -553,10 +647,13 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, dt = cpu_sample(models, args, os.cpu_count())
+        v, dt, ev, lw = cpu_sample(models, args, os.cpu_count())
         cpu = {"value": v, "unit": "packets/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "%d models x %d packets of the workload, CPU restatement (%.1f s)" %
-               (min(args.cpu_models, len(models)), args.cpu_packets, dt)}
+               "interactions_per_s": ev / dt, "longest_walk": lw,
+               "sample": "%d models x %d packets of the workload (Monte Carlo seed %d), CPU "
+                         "restatement in %d single-threaded workers (%.1f s)" %
+               (min(args.cpu_models, len(models)), args.cpu_packets, args.seed,
+                os.cpu_count(), dt)}
 
     K, P = plan.opts.nepoch, plan.opts.npilot
     # start + (prep + transport) per pass and epoch + two continuation launches +

@@ -16,8 +16,10 @@
 #define MC_EUNIT_SHIFT 20
 #define MC_MAX_SPEC 4
 #define MC_MAX_EPOCH 24
-#define MC_NSTAT 128
-#define MC_LSTAT 32     // per-launch slots: (t_start, t_end, max events, parked)
+#define MC_NSTAT 256
+#define MC_LSTAT 32     // per-launch slots from here, MC_LSTRIDE each: (t_start, t_end,
+                        // max events, parked, interactions, crossings, deposits)
+#define MC_LSTRIDE 8
 #define MC_MAX_LAUNCH 24
 
 // pdspy physical constants (pdspy/constants/physics.py:1-15).

@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
             tot = c < P.park_in_cap ? c : P.park_in_cap;
         }
         s_total = tot;
-        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
+        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + MC_LSTRIDE * P.lslot), (unsigned long long)globaltimer());
     }
     const float* tab = P.fpool;
     if (P.use_smem) {
@@ -1259,11 +1259,16 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     long long pk = warp_sum(cnt.parked);
+    const long long le = warp_sum(cnt.events), lc = warp_sum(cnt.crossings),
+                    ld = warp_sum(cnt.absorb + cnt.mrw);
     if (lane == 0) {
-        int64_t* L = P.stats + MC_LSTAT + 4 * P.lslot;
+        int64_t* L = P.stats + MC_LSTAT + MC_LSTRIDE * P.lslot;
         atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
         atomicMax((unsigned long long*)(L + 2), (unsigned long long)mx);
         if (pk) atomicAdd((unsigned long long*)(L + 3), (unsigned long long)pk);
+        if (le) atomicAdd((unsigned long long*)(L + 4), (unsigned long long)le);
+        if (lc) atomicAdd((unsigned long long*)(L + 5), (unsigned long long)lc);
+        if (ld) atomicAdd((unsigned long long*)(L + 6), (unsigned long long)ld);
     }
 }
 
@@ -1489,7 +1494,7 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         s_stop = (*(volatile long long*)(P.stats + ST_STOP) != 0) ? 1 : 0;
         long long c = (long long)*(volatile const unsigned long long*)P.park_in_count;
         s_total = c < P.park_in_cap ? c : P.park_in_cap;
-        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + 4 * P.lslot), (unsigned long long)globaltimer());
+        atomicMin((unsigned long long*)(P.stats + MC_LSTAT + MC_LSTRIDE * P.lslot), (unsigned long long)globaltimer());
     }
     const float* tab = P.fpool;
     if (P.use_smem) {
@@ -1566,9 +1571,13 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
                              ST_MRW, ST_LATE, ST_PARKED};
         for (int i = 0; i < 9; ++i)
             if (v[i]) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)v[i]);
-        int64_t* L = P.stats + MC_LSTAT + 4 * P.lslot;
+        int64_t* L = P.stats + MC_LSTAT + MC_LSTRIDE * P.lslot;
         atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
         atomicMax((unsigned long long*)(L + 2), (unsigned long long)cnt.maxev);
+        if (cnt.events) atomicAdd((unsigned long long*)(L + 4), (unsigned long long)cnt.events);
+        if (cnt.crossings) atomicAdd((unsigned long long*)(L + 5), (unsigned long long)cnt.crossings);
+        if (cnt.absorb + cnt.mrw)
+            atomicAdd((unsigned long long*)(L + 6), (unsigned long long)(cnt.absorb + cnt.mrw));
     }
 }
 
@@ -1673,7 +1682,7 @@ __global__ void mc_temperature_kernel(TempParams P) {
 
 __global__ void mc_start_kernel(int64_t* stats) {
     stats[ST_T0] = (int64_t)globaltimer();
-    for (int l = 0; l < MC_MAX_LAUNCH; ++l) stats[MC_LSTAT + 4 * l] = 0x7fffffffffffffffLL;
+    for (int l = 0; l < MC_MAX_LAUNCH; ++l) stats[MC_LSTAT + MC_LSTRIDE * l] = 0x7fffffffffffffffLL;
 }
 
 __global__ void mc_finish_kernel(int64_t* stats, int64_t packets) {

@@ -234,16 +234,22 @@ class ThermalPlan:
 
     def raw_stats(self):
         o = self.layout.stats_offset
-        return self.workspace[o:o + 8 * 128].view(torch.int64)
+        return self.workspace[o:o + 8 * 256].view(torch.int64)
 
     def launch_stats(self):
         """Per transport launch: (duration ms, longest packet in events, parked packets)."""
+        return [(d["ms"], d["longest"], d["parked"]) for d in self.launch_counts()]
+
+    def launch_counts(self):
+        """Per transport launch of the last run: device-clock duration (ms), longest packet
+        (events), packets parked, interactions, crossings and deposits."""
         r = self.raw_stats().cpu().numpy()
         out = []
         for l in range(24):
-            t0, t1, mx, pk = r[32 + 4 * l: 36 + 4 * l]
+            t0, t1, mx, pk, ev, cr, dep = r[32 + 8 * l: 39 + 8 * l]
             if t1 > 0 and t0 < (1 << 62):
-                out.append(((t1 - t0) / 1e6, int(mx), int(pk)))
+                out.append(dict(ms=(t1 - t0) / 1e6, longest=int(mx), parked=int(pk),
+                                events=int(ev), crossings=int(cr), deposits=int(dep)))
         return out
 
     def set_timelimit(self, seconds):
