@@ -21,9 +21,9 @@ over an MPI pool).  ``lnprob_batched`` evaluates a whole ensemble in one go:
      galario's method) with the (x0, y0) offset, and lnlike's visibility term.
 
 Scope: the "truncated" power-law disk with an optional "ulrich-extended" envelope (its
-centrifugal radius = R_disk, as YSOModel does unless rcent_ne_rdisk), the visibility
-likelihood (lnlike's image and SED terms need data products outside this path), and one
-dust model for disk and envelope (pdspy's DustGenerator tables are not available).  The
+centrifugal radius = R_disk, as YSOModel does unless rcent_ne_rdisk), lnlike's visibility,
+image (beam-convolved model images) and SED (free-free added, reddened, log10) terms, and
+one dust model for disk and envelope (pdspy's DustGenerator tables are not available).  The
 free-free point source run_disk_model adds to the real part of the visibilities
 (:325-334, pdspy/spectroscopy/freefree.py, interferometry/model.py:102-104) is added the
 same way.
@@ -58,6 +58,7 @@ def base_parameters():
         "y0": e(0., -0.1, 0.1), "dpc": e(140., 1., 1e6, prior="box", sigma=0.),
         "flux_unc1": e(1., 0.5, 1.5, prior="box", sigma=0.),
         "logF_nu_ff": e(-20., -30., 0.), "lognu_turn": e(0., -1., 2.), "pl_turn": e(0.6, 0., 2.),
+        "Ak": e(0., 0., 1.),
     }
 
 
@@ -161,6 +162,88 @@ def freefree_real(u, v, freq, p):
     return f * np.cos(2 * 3.14159 * (np.asarray(u) * x0 + np.asarray(v) * y0))
 
 
+def gaussian_beam(bmaj, bmin, bpa, pixelsize):
+    """The beam run_disk_model convolves model images with (run_disk_model.py:468-472):
+    pdspy's misc.gaussian2d (misc/gaussian2d.py:3-8) on a 512 x 512 pixel grid, sigmas
+    bmaj/2.355 and bmin/2.355 in pixels, position angle (90 - bpa) degrees, peak 1."""
+    x, y = np.meshgrid(np.linspace(-256, 255, 512), np.linspace(-256, 255, 512))
+    sx = bmaj / 2.355 / pixelsize
+    sy = bmin / 2.355 / pixelsize
+    pa = (90 - bpa) * np.pi / 180.
+    xp = x * np.cos(pa) - y * np.sin(pa)
+    yp = x * np.sin(pa) + y * np.cos(pa)
+    return np.exp(-1 * xp ** 2 / (2 * sx ** 2)) * np.exp(-1 * yp ** 2 / (2 * sy ** 2))
+
+
+def convolve_same(plane, kernel, device=None):
+    """scipy.signal.fftconvolve(plane, kernel, mode="same") in float64 with torch.fft on
+    ``device``: the linear convolution through zero-padded transforms, cropped to the
+    plane's shape about the centre of the full result."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    a = torch.as_tensor(np.asarray(plane, dtype=np.float64), device=dev)
+    k = torch.as_tensor(np.asarray(kernel, dtype=np.float64), device=dev)
+    full = (a.shape[0] + k.shape[0] - 1, a.shape[1] + k.shape[1] - 1)
+    f = torch.fft.irfft2(torch.fft.rfft2(a, s=full) * torch.fft.rfft2(k, s=full), s=full)
+    y0 = (full[0] - a.shape[0]) // 2
+    x0 = (full[1] - a.shape[1]) // 2
+    return f[y0:y0 + a.shape[0], x0:x0 + a.shape[1]].cpu().numpy()
+
+
+def redden(wave_um, flux, Av, law=None):
+    """pdspy's dust.redden (dust/redden.py:6-63): flux / 10**(Av coeff / 2.5) with coeff the
+    extinction law interpolated linearly in log-log (extrapolated from the end segments).
+    ``law`` = (wavelengths in um, coefficients) of the tabulated law pdspy reads from its
+    data files (McClure 2009 for run_disk_model); with Av = 0 the flux passes unchanged and
+    no table is needed."""
+    flux = np.asarray(flux, dtype=np.float64)
+    if Av == 0:
+        return flux / 10. ** (0. * np.ones_like(flux) / 2.5)
+    if law is None:
+        raise ValueError("redden: Av = %g needs the extinction law table (wavelengths, "
+                         "coefficients)" % Av)
+    lw = np.log10(np.asarray(law[0], dtype=np.float64))
+    lc = np.log10(np.asarray(law[1], dtype=np.float64))
+    order = np.argsort(lw)
+    lw, lc = lw[order], lc[order]
+    x = np.log10(np.asarray(wave_um, dtype=np.float64))
+    y = np.interp(x, lw, lc)
+    lo, hi = x < lw[0], x > lw[-1]
+    y[lo] = lc[0] + (lc[1] - lc[0]) / (lw[1] - lw[0]) * (x[lo] - lw[0])
+    y[hi] = lc[-2] + (lc[-1] - lc[-2]) / (lw[-1] - lw[-2]) * (x[hi] - lw[-2])
+    return flux / 10. ** (Av * 10. ** y / 2.5)
+
+
+def model_image(m, p, img_set, device):
+    """run_disk_model's model image for one image data set (run_disk_model.py:457-476):
+    run_image at the set's wavelength (1e5 scattering packets, mc_scat_maxtauabs 5),
+    convolved with the set's beam; returns the Image.  (The reference reads the beam's
+    second pixel size from an undefined name, ``image["pixelsize"]``; the set's pixel size
+    is used for both axes here.)"""
+    lam = img_set["lam"]
+    im = image.run_image(m, name=lam, nphot=1e5, npix=int(img_set["npix"]),
+                         pixelsize=float(img_set["pixelsize"]),
+                         lam=[float(lam)], incl=p["i"], pa=p["pa"], dpc=p["dpc"],
+                         mc_scat_maxtauabs=5)
+    beam = gaussian_beam(img_set["bmaj"], img_set["bmin"], img_set["bpa"],
+                         float(img_set["pixelsize"]))
+    im.image = convolve_same(im.image[:, :, 0, 0], beam, device).reshape(im.image.shape)
+    return im
+
+
+def model_sed(m, p, spectrum, extinction_law=None):
+    """run_disk_model's model SED (run_disk_model.py:480-504): run_sed at the data's
+    wavelengths (1e4 packets, scattering at every wavelength, mc_scat_maxtauabs 5), plus the
+    free-free spectrum, reddened by A_k, as log10 flux."""
+    m.set_camera_wavelength(np.asarray(spectrum.wave, dtype=np.float64))
+    sed = image.run_sed(m, name="SED", nphot=1e4, loadlambda=True, incl=p["i"], pa=p["pa"],
+                        dpc=p["dpc"], camera_scatsrc_allfreq=True, mc_scat_maxtauabs=5)
+    sed.flux = sed.flux + freefree(sed.freq, p.get("F_nu_ff", 0.0), p.get("nu_turn", 1.0) * 1e9,
+                                   p.get("pl_turn", 0.6))
+    sed.flux = redden(sed.wave, sed.flux, p.get("Ak", 0.0), law=extinction_law)
+    sed.flux = np.log10(sed.flux)
+    return sed
+
+
 def _lnlike_vis(re, im, data):
     """lnlike's visibility term (utils/emcee.py:31-43), numerically as pdspy writes it."""
     w = data.weights
@@ -194,12 +277,19 @@ def model_visibilities(m, p, vis_set, device, pad=2, nphot_image=1e5):
 
 
 def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=None,
-                   nphot=1e6, device=None, pad=2, timelimit=3600.0, seed=0):
+                   nphot=1e6, device=None, pad=2, timelimit=3600.0, seed=0, images=None,
+                   spectra=None, extinction_law=None):
     """lnprob of every walker (rows of P, the free parameters in sorted key order as
     pdspy's lnprob orders them) with one batched thermal launch; returns float64 [nwalker].
 
     timelimit: seconds of device time per walker (one number or one per row of P); a
     walker whose thermal run has not finished in time scores -inf alone.
+
+    images: list of dicts with "data" (an Image with ``image`` and ``unc``), "npix",
+    "pixelsize", "lam", "bmaj", "bmin", "bpa" (pdspy's images[...][j]); spectra: dict with
+    "total" (a Spectrum of log10 flux with ``unc`` at the data wavelengths).  They add
+    lnlike's image and SED terms (utils/emcee.py:45-58).  extinction_law: the (wavelength
+    um, coefficient) table redden needs when A_k is not 0.
 
     visibilities: list of dicts with "data" (vis.UVData plus ``freq``), "npix" and
     "pixelsize" (arcsec), one per visibility set (pdspy's visibilities["data"][j],
@@ -242,5 +332,13 @@ def lnprob_batched(P, visibilities, parameters, priors=None, dust=None, lam_um=N
             vs = dict(vs, index=j + 1)
             re, im = model_visibilities(m, p, vs, dev, pad=pad)
             ll += _lnlike_vis(re, im, vs["data"])
+        for img_set in images or []:
+            mi = model_image(m, p, img_set, dev)
+            d = img_set["data"]
+            ll += -0.5 * (np.sum((d.image - mi.image) ** 2 / d.unc ** 2))
+        if spectra and "total" in spectra:
+            sed = model_sed(m, p, spectra["total"], extinction_law)
+            d = spectra["total"]
+            ll += -0.5 * (np.sum((d.flux - sed.flux) ** 2 / d.unc ** 2))
         out[w] = lp + ll
     return out

@@ -291,6 +291,25 @@ def run_image(model, name=None, nphot=1e6, npix=256, pixelsize=1.0, lam="1300",
     return model.images[name]
 
 
+def run_visibilities(model, name=None, nphot=1e6, npix=256, pixelsize=1.0, lam="1300",
+                     loadlambda=False, incl=0, pa=0, phi=0, dpc=1, nostar=False, **keywords):
+    """``Model.run_visibilities`` for code="gb300" (Model.py:682-721): the image of
+    run_image (Jy/pixel at ``dpc``, arcsec offsets) transformed by imtovis on the GPU;
+    fills ``model.visibilities[name]`` and leaves ``model.images`` untouched, as the
+    reference does."""
+    from .vis import imtovis
+    saved = model.images.get("__run_visibilities__")
+    im = run_image(model, name="__run_visibilities__", nphot=nphot, npix=npix,
+                   pixelsize=pixelsize, lam=lam, loadlambda=loadlambda, incl=incl, pa=pa,
+                   phi=phi, dpc=dpc, nostar=nostar, **keywords)
+    if saved is None:
+        del model.images["__run_visibilities__"]
+    else:
+        model.images["__run_visibilities__"] = saved
+    model.visibilities[name] = imtovis(im)
+    return model.visibilities[name]
+
+
 def run_sed(model, name=None, nphot=1e6, incl=0, pa=0, phi=0, dpc=1, loadlambda=False,
             npix=128, max_refine=6, refine_factor=0.5, **keywords):
     """``Model.run_sed`` for code="gb300": flux in Jy at ``dpc`` of an image covering the

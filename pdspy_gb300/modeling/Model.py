@@ -1,8 +1,8 @@
 """Generic model; mirrors pdspy/modeling/Model.py with a "gb300" code path.
 
-``run_thermal``, ``run_scattering``, ``run_image`` and ``run_sed`` keep the reference's
-signatures and string dispatch on ``code`` (Model.py:69-72, :275-278, :345-348,
-:600-603).  ``code="gb300"`` (the
+``run_thermal``, ``run_scattering``, ``run_image``, ``run_sed`` and ``run_visibilities``
+keep the reference's signatures and string dispatch on ``code`` (Model.py:69-72,
+:275-278, :345-348, :600-603, :672-675).  ``code="gb300"`` (the
 default here) runs the CUDA backend; "radmc3d" and "hyperion" name external programs
 that are not part of this package and raise NotImplementedError.
 """
@@ -41,4 +41,10 @@ class Model:
         if code == "gb300":
             from ..image import run_sed
             return run_sed(self, name=name, nphot=nphot, **keywords)
+        raise NotImplementedError("code=%r is an external program; use code='gb300'" % code)
+
+    def run_visibilities(self, name=None, nphot=1e6, code="gb300", **keywords):
+        if code == "gb300":
+            from ..image import run_visibilities
+            return run_visibilities(self, name=name, nphot=nphot, **keywords)
         raise NotImplementedError("code=%r is an external program; use code='gb300'" % code)

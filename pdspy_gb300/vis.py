@@ -167,6 +167,30 @@ class Visibilities:
         self.real, self.imag, self.weights = real, imag, weights
 
 
+def imtovis(image, device=None):
+    """``imtovis`` (pdspy/imaging/imtovis.py:6-27) on the GPU: the visibilities on the
+    image's own Fourier grid, per frequency fftshift(fft2(ifftshift(plane))) in complex128
+    (cuFFT through torch.fft, a plain library transform), u and v from
+    fftshift(fftfreq(n, pixel [rad])), flattened row by row as pdspy's meshgrid/reshape does
+    (u runs along x, v along y), unit weights.  ``image`` is an Image with
+    ``image[ny, nx, nfreq, 1]`` in Jy/pixel and ``x``/``y`` in arcsec."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    img = torch.as_tensor(np.asarray(image.image[:, :, :, 0], dtype=np.float64), device=dev)
+    ny, nx, nf = img.shape
+    planes = img.permute(2, 0, 1)                                  # [nfreq, ny, nx]
+    V = torch.fft.fftshift(torch.fft.fft2(torch.fft.ifftshift(planes, dim=(-2, -1))),
+                           dim=(-2, -1))
+    real = V.real.reshape(nf, ny * nx).T.contiguous().cpu().numpy()
+    imag = V.imag.reshape(nf, ny * nx).T.contiguous().cpu().numpy()
+    x = np.asarray(image.x, dtype=np.float64)
+    y = np.asarray(image.y, dtype=np.float64)
+    uu = np.fft.fftshift(np.fft.fftfreq(x.size, (x[1] - x[0]) * arcsec))
+    vv = np.fft.fftshift(np.fft.fftfreq(y.size, (y[1] - y[0]) * arcsec))
+    u, v = np.meshgrid(uu, vv)
+    return Visibilities(u.reshape(-1), v.reshape(-1), np.atleast_1d(image.freq), real, imag,
+                        np.ones(real.shape))
+
+
 def interpolate_model(u, v, freq, model, dRA=0.0, dDec=0.0, code="fft", pad=1, device=None):
     """``interpolate_model`` (pdspy/interferometry/interpolate_model.py:11-57) on the GPU:
     model visibilities of an Image (``image[ny, nx, nfreq, 1]`` Jy/pixel, ``x``/``y`` in

@@ -70,3 +70,33 @@ def test_freefree_matches_pdspy_formula():
     ff = fitting.freefree(2.3e11, F, 5e9, pl)
     pt = ff * np.exp(-2 * 3.14159 * (0 + 1j * (u * 0.02 * arcsec + v * -0.01 * arcsec)))
     assert np.allclose(fitting.freefree_real(u, v, [2.3e11], p), pt.real, rtol=1e-14)
+
+
+def test_beam_convolution_matches_scipy_fftconvolve():
+    """run_disk_model's beam convolution (run_disk_model.py:468-476): the beam of pdspy's
+    gaussian2d on the 512 x 512 grid, and fftconvolve(..., mode="same") of a model plane."""
+    import scipy.signal
+    beam = fitting.gaussian_beam(0.12, 0.08, 30.0, 0.02)
+    assert beam.shape == (512, 512) and beam.max() == 1.0
+    rng = np.random.default_rng(2)
+    for shape in [(64, 64), (63, 80)]:
+        plane = rng.random(shape)
+        got = fitting.convolve_same(plane, beam, device=torch.device("cpu"))
+        ref = scipy.signal.fftconvolve(plane, beam, mode="same")
+        assert got.shape == ref.shape
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_redden_follows_pdspy():
+    """dust.redden (dust/redden.py:6-63): identity at A = 0, otherwise the law interpolated
+    in log-log with extrapolation, as interp1d(fill_value="extrapolate") does."""
+    from scipy.interpolate import interp1d
+    wave = np.logspace(-0.5, 3.5, 40)
+    flux = np.logspace(-3, 1, 40)
+    assert np.array_equal(fitting.redden(wave, flux, 0.0), flux)
+    lw = np.array([1.0, 2.2, 5.0, 20.0, 100.0])
+    lc = np.array([7.0, 1.0, 0.45, 0.3, 0.05])
+    got = fitting.redden(wave, flux, 0.4, law=(lw, lc))
+    f = interp1d(np.log10(lw), np.log10(lc), fill_value="extrapolate")
+    ref = flux / 10. ** (0.4 * 10. ** f(np.log10(wave)) / 2.5)
+    assert np.allclose(got, ref, rtol=1e-12, atol=0)

@@ -111,3 +111,31 @@ def test_image_flux_is_omega_times_pixel_sum(cuda):
     got = plan.flux(img).cpu().numpy()
     expect = img.sum(dim=(1, 2)).cpu().numpy() * (pixel_cm / K.pc) ** 2
     assert np.allclose(got, expect, rtol=1e-12, atol=0)
+
+
+def test_run_visibilities_is_imtovis_of_the_image(cuda):
+    """Model.run_visibilities (Model.py:682-721): the image of run_image transformed like
+    pdspy's imtovis (imaging/imtovis.py:6-27): fftshift(fft2(ifftshift(plane))) per
+    frequency, u/v from fftshift(fftfreq(n, pixel)), flattened row by row, unit weights.
+    Checked against numpy's transform of the same image (complex128 both)."""
+    m = _cases.image_model("disk", nr=12, ntheta=12)
+    kw = dict(nphot=2000, npix=32, pixelsize=0.05, lam=[1300.0, 870.0], incl=40.0, pa=20.0,
+              dpc=140.0)
+    im = m.run_image(name="img", **kw)
+    vis = m.run_visibilities(name="vis", **kw)
+    assert "vis" in m.visibilities and list(m.images) == ["img"]
+    n = 32
+    for i in range(2):
+        ref = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(im.image[:, :, i, 0])))
+        scale = np.abs(ref).max()
+        assert np.abs(vis.real[:, i] - ref.real.reshape(-1)).max() <= 1e-12 * scale
+        assert np.abs(vis.imag[:, i] - ref.imag.reshape(-1)).max() <= 1e-12 * scale
+    uu = np.fft.fftshift(np.fft.fftfreq(n, (im.x[1] - im.x[0]) * K.arcsec))   # as pdspy
+    vv = np.fft.fftshift(np.fft.fftfreq(n, (im.y[1] - im.y[0]) * K.arcsec))
+    u, v = np.meshgrid(uu, vv)
+    assert np.array_equal(vis.u, u.reshape(-1)) and np.array_equal(vis.v, v.reshape(-1))
+    assert vis.real.shape == (n * n, 2) and np.all(vis.weights == 1.0)
+    assert np.allclose(vis.freq, im.freq)
+    # the zero-spacing visibility is the total flux
+    k = (n // 2) * n + n // 2
+    assert vis.real[k, 0] == pytest.approx(im.image[:, :, 0, 0].sum(), rel=1e-12)
