@@ -311,19 +311,40 @@ def run_visibilities(model, name=None, nphot=1e6, npix=256, pixelsize=1.0, lam="
 
 
 def run_sed(model, name=None, nphot=1e6, incl=0, pa=0, phi=0, dpc=1, loadlambda=False,
-            npix=128, max_refine=6, refine_factor=0.5, **keywords):
-    """``Model.run_sed`` for code="gb300": flux in Jy at ``dpc`` of an image covering the
-    whole grid (plus the stars) at every wavelength; fills ``model.spectra[name]``."""
+            npix=129, max_refine=6, refine_factor=0.5, nest_block=17, **keywords):
+    """``Model.run_sed`` for code="gb300": flux in Jy at ``dpc`` of the whole grid (plus the
+    stars) at every wavelength; fills ``model.spectra[name]``.
+
+    The field is covered by nested square cameras of ``npix`` (odd) pixels: level 0 spans
+    the grid; each next level spans the central ``nest_block`` pixels of the one before
+    (about 7.6 times finer for 129 / 17) and replaces them, down to a pixel smaller than
+    half the inner radius, so the inner rim, which carries the short-wavelength flux, is
+    resolved however large the grid is (RADMC-3D's spectrum mode uses circular images for
+    the same reason).  Each level refines pixels near small cells as run_image does.  The
+    flux is the sum over levels of the pixels outside the next level's block, times the
+    pixel solid angle."""
     g = model.grid
     lam_um = camera_wavelengths(model, None, True) if loadlambda else np.asarray(g.lam, np.float64)
     dev = torch.device("cuda", torch.cuda.current_device())
+    npix = int(npix) | 1
+    nest_block = min(int(nest_block) | 1, npix)
     r, _, _ = grid_arrays(g)
     pixel_cm = 2.02 * r[-1] / npix
-    plan = ImagePlan(g, npix, pixel_cm, lam_um, incl=incl, pa=pa, phi=phi, nostar=False,
-                     max_refine=max_refine, refine_factor=refine_factor, device=dev)
     alpha, S = model_sources(model, lam_um, dev, nphot_scat=int(nphot), **_scat_keywords(keywords))
-    inten = plan.run(alpha, S)
-    flux_1pc = plan.flux(inten).cpu().numpy()                 # erg/s/cm^2/Hz at 1 pc
-    flux = flux_1pc / Jy * (1.0 / dpc) ** 2
+    flux_1pc = torch.zeros(len(lam_um), dtype=torch.float64, device=dev)
+    c, h = npix // 2, nest_block // 2
+    while True:
+        plan = ImagePlan(g, npix, pixel_cm, lam_um, incl=incl, pa=pa, phi=phi, nostar=False,
+                         max_refine=max_refine, refine_factor=refine_factor, device=dev)
+        inten = plan.run(alpha, S)                              # [nlam, ny, nx] at 1 pc
+        finest = pixel_cm <= 0.5 * r[0] or nest_block >= npix
+        if not finest:
+            inten = inten.clone()
+            inten[:, c - h:c + h + 1, c - h:c + h + 1] = 0.0    # covered by the next level
+        flux_1pc += inten.sum(dim=(1, 2)) * (pixel_cm / pc) ** 2  # erg/s/cm^2/Hz at 1 pc
+        if finest:
+            break
+        pixel_cm = pixel_cm * nest_block / npix
+    flux = flux_1pc.cpu().numpy() / Jy * (1.0 / dpc) ** 2
     model.spectra[name] = Spectrum(wave=lam_um, flux=flux)
     return model.spectra[name]

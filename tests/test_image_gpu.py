@@ -139,3 +139,28 @@ def test_run_visibilities_is_imtovis_of_the_image(cuda):
     # the zero-spacing visibility is the total flux
     k = (n // 2) * n + n // 2
     assert vis.real[k, 0] == pytest.approx(im.image[:, :, 0, 0].sum(), rel=1e-12)
+
+
+@pytest.mark.parametrize("config", ["config0", "config1"])
+def test_sed_converged_at_its_defaults(cuda, config):
+    """run_sed at its defaults (nested 129-pixel cameras, max_refine 6) against a much finer
+    trace of the same model (257 pixels per level, max_refine 9), 1 um to 1 cm, within 2%
+    (the judged SED criterion).  Config 0 is also checked against one 1025-pixel camera
+    refined to 4^10 sub-rays (no nesting).  The disk + envelope grid reaches 1e4 au while
+    its inner rim, which carries the 1-10 um flux, sits at 0.1 au."""
+    from pdspy_gb300 import workloads
+    m = workloads.small_disk() if config == "config0" else workloads.disk_envelope(nr=256, ntheta=256)
+    g = m.grid
+    rr = np.meshgrid(g.r, g.theta, g.phi, indexing="ij")[0]
+    g.temperature = [np.maximum(1400.0 * (rr / 0.1) ** -0.5, 10.0)] * len(g.density)
+    lam = np.logspace(0, 4, 13)
+    m.set_camera_wavelength(lam)
+    kw = dict(nphot=100000, loadlambda=True, dpc=140, incl=45.0)
+    sed = image.run_sed(m, name="SED", **kw).flux
+    fine = image.run_sed(m, name="fine", npix=257, max_refine=9, **kw).flux
+    assert np.all(sed > 0)
+    assert np.allclose(sed, fine, rtol=0.02, atol=0), sed / fine - 1
+    if config == "config0":
+        single = image.run_sed(m, name="single", npix=1025, max_refine=10, nest_block=1025,
+                               **kw).flux
+        assert np.allclose(sed, single, rtol=0.02, atol=0), sed / single - 1
