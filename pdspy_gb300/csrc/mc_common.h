@@ -21,6 +21,9 @@
                         // max events, parked, interactions, crossings, deposits)
 #define MC_LSTRIDE 8
 #define MC_MAX_LAUNCH 24
+// static shared memory of the continuation kernel's batched walks: 17 fields x 32 lanes
+// of 4 bytes per warp, 8 warps per block of at most 256 threads
+#define MC_TAIL_SMEM (8 * 17 * 32 * 4)
 
 // pdspy physical constants (pdspy/constants/physics.py:1-15).
 #define MC_C_LIGHT 2.99792458e10

@@ -445,7 +445,7 @@ struct LanePol {
 struct WarpPol {
     int lane;
     // random numbers of interactions n0 .. n0 + 31, lane l holding n0 + l
-    bool rv;
+    bool rv, rmv;
     uint32_t n0;
     EvR re;
     SecR rs;
@@ -471,7 +471,7 @@ struct WarpPol {
     // the packet's own-deposit cache, replicated in every lane
     McOwn own;
     __device__ __forceinline__ explicit WarpPol(int l, int gc, float g)
-        : lane(l), rv(false), n0(0), gconst(gc), g0(g), cm(-1), cc(-1), ce(-1), cv(-1),
+        : lane(l), rv(false), rmv(false), n0(0), gconst(gc), g0(g), cm(-1), cc(-1), ce(-1), cv(-1),
           cvalid(0u) { own_init(own); }
     __device__ __forceinline__ void own_reset() { own_init(own); }
     __device__ __forceinline__ void own_add(int sc, long long units) { ::own_add(own, sc, units); }
@@ -563,12 +563,19 @@ struct WarpPol {
             const uint32_t m = n + (uint32_t)lane;
             re = ev_of(mc_block(r, m, MC_RS_EVENT, k0, k1));
             rs = sec_of(mc_block(r, m, MC_RS_SECOND, k0, k1));
-            rm = mrw_of(mc_block(r, m, MC_RS_MRW, k0, k1));
+            rmv = false;   // the MRW stream is drawn when a jump first needs it
             iso_of(re, ikx, iky, ikz);
             hgmu = gconst ? hg_mu(g0, re.umu) : 0.0f;
             rv = true;
         }
         return (int)(n - n0);
+    }
+    // random numbers of interactions n .. n + 31, lane l holding n + l
+    __device__ __forceinline__ void refill_at(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
+        if (!rv || n0 != n) {
+            rv = false;
+            slot(r, n, k0, k1);
+        }
     }
     __device__ __forceinline__ EvR ev(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
         const int l = slot(r, n, k0, k1);
@@ -591,6 +598,10 @@ struct WarpPol {
     }
     __device__ __forceinline__ MrwR mrwd(const McRng& r, uint32_t n, uint32_t k0, uint32_t k1) {
         const int l = slot(r, n, k0, k1);
+        if (!rmv) {
+            rm = mrw_of(mc_block(r, n0 + (uint32_t)lane, MC_RS_MRW, k0, k1));
+            rmv = true;
+        }
         MrwR o;
         o.uy = __shfl_sync(0xffffffffu, rm.uy, l);
         o.jmu = __shfl_sync(0xffffffffu, rm.jmu, l);
@@ -1483,6 +1494,402 @@ __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const M
     return 1;
 }
 
+// Per-warp shared staging of the batch's chains: field f of lane l at sb[f * 32 + l].  The
+// chain loops read their inputs as broadcasts, so the loads are issued ahead of the chain.
+enum { TB_A0, TB_A1, TB_A2, TB_A3, TB_A4, TB_A5, TB_LAM, TB_ALPHA, TB_XH, TB_XL, TB_YH, TB_YL,
+       TB_ZH, TB_ZL, TB_DS, TB_DM, TB_FR, TB_NF };
+
+// Interactions of a trapped packet, up to 32 at a time across the warp (lane l takes the
+// batch's interaction l), with exactly the decisions and the arithmetic of tail_fast_run's
+// steps in the same order.  Everything an interaction needs that does not depend on the
+// packet's path so far is computed by its own lane: the random numbers, the isotropic
+// direction, the Henyey-Greenstein cosine and the reemission wavelength.  What does
+// depend on the path runs as short chains over the lanes' values:
+//   1. the wavelength chain: interaction l absorbs or scatters at the wavelength left by
+//      the last absorption before it; each lane has precomputed its reemission (at a guess
+//      of the packet's own deposits in the cell, checked in step 6) and the extinction and
+//      scattering coefficients there, so a link is a compare and a select;
+//   2. the directions: after an absorption the lane's isotropic direction, after a
+//      scattering the previous direction rotated (rounds over runs of scatterings);
+//   3. the positions: the moves' products are formed per lane, the double-single sums
+//      are chained in interaction order;
+//   4. per lane at its position: the wall distance (safety-distance refresh and MRW try),
+//      the Rosseland mean at the own deposits of that moment, and whether a try jumps;
+//   5. the safety-distance / distance-bound chain with the MRW tries, which marks the
+//      interactions that need a wall solve; those lanes solve their walls side by side;
+//   6. the exact reemission check.
+// The batch is committed up to the first interaction that leaves this scheme: a crossing
+// (applied here from its lane's wall solve), an MRW jump, an interaction placed beyond the
+// wall by rounding, or an empty cell (each left to one tail_fast_run step), or a reemission
+// whose guess was wrong (committed with the exact wavelength, the rest recomputed).  The
+// deposits of the committed absorptions go to the cell in one atomic (int64 sums do not
+// depend on the order).  Returns like tail_fast_run.
+__device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const McModel& M,
+                                              const DustTabs& T, Cnt& cnt, WarpPol& pol,
+                                              TailCell& tc, float* __restrict__ sb, int budget,
+                                              int& steps) {
+    const unsigned FULL = 0xffffffffu;
+    const int nl = P.nl;
+    const uint32_t k0 = P.key0, k1 = P.key1;
+    const int64_t base = M.cell_off;
+    const int l = pol.lane;
+    steps = 0;
+    // batch size: 16 after a crossing or an MRW jump (half the batches end within 10
+    // interactions), 32 after a batch committed whole
+    int bcap = 16;
+    while (steps < budget) {
+        // room for one more step after the batch, all interactions on the same side of
+        // late_after, none reaching the interaction cap
+        int B = budget - steps - 1;
+        if (B > bcap) B = bcap;
+        const long long ne = p.nevents;
+        if (P.late_after > 0 && ne < P.late_after && ne + B > P.late_after)
+            B = (int)(P.late_after - ne);
+        bool ok = p.ir >= 0 && B >= 1 && ne + B < (long long)P.max_inter;
+        if (ok) {
+            if (p.ir != tc.ir || p.itv != tc.itv || p.ip != tc.ip || p.epoch != tc.epoch) {
+                tc.c = cell_of_s(M, p);
+                tc.ir = p.ir; tc.itv = p.itv; tc.ip = p.ip; tc.epoch = p.epoch;
+                tc.rho = __ldg(P.rho + base + tc.c);
+                tc.wq = __ldg(P.wq + base + tc.c);
+                tc.q = P.q[(int64_t)p.epoch * P.qstride + base + tc.c];
+            }
+            float a0 = 0.0f;
+            a0 = a0 + tc.rho * T.kext[p.lam];
+            ok = a0 > 0.0f;
+        }
+        if (!ok) {
+            int s1 = 0;
+            const int r = tail_fast_run(p, P, M, T, cnt, pol, tc, 1, s1);
+            steps += s1;
+            if (r != 1) return r;
+            continue;
+        }
+        const WallsCell& W = pol.cell_walls(M, P.fpool, p);
+        const int c = tc.c;
+        const float rh = tc.rho, wq = tc.wq;
+        const float2 q = tc.q;
+        pol.refill_at(p.rng, (uint32_t)p.nevents, k0, k1);
+        long long u0 = 0;
+#pragma unroll
+        for (int i = 0; i < MC_OWN; ++i)
+            if (pol.own.sc[i] == c) u0 = pol.own.u[i];
+
+        // reemission of this lane's interaction if it is an absorption, at a guess of the own
+        // deposits (half of the earlier interactions absorbed)
+        const long long ug = u0 + ((long long)(l / 2 + 1) << MC_EUNIT_SHIFT);
+        float qg = q.x + pol.rs.uq * q.y;
+        qg = qg + (float)ug * wq;
+        int gj;
+        float gw;
+        mc_row_search(T.F, qg, gj, gw);
+        const int grow = gj + ((pol.rs.urow < gw) ? 1 : 0);
+        const int glam = mc_cdf_search(T.cdf + (size_t)grow * nl, nl, pol.rs.ucdf);
+        float ga = 0.0f;
+        ga = ga + rh * T.kext[glam];
+        float gs = 0.0f;
+        gs = gs + rh * T.ksca[glam];
+
+        // 1. wavelength chain
+        int cl = p.lam;
+        float ca = 0.0f;
+        ca = ca + rh * T.kext[cl];
+        float cs = 0.0f;
+        cs = cs + rh * T.ksca[cl];
+        unsigned amask = 0u;
+        sb[TB_A0 * 32 + l] = pol.re.ua;
+        sb[TB_A1 * 32 + l] = __int_as_float(glam);
+        sb[TB_A2 * 32 + l] = ga;
+        sb[TB_A3 * 32 + l] = gs;
+        __syncwarp();
+#pragma unroll 4
+        for (int j = 0; j < B; ++j) {
+            const float ua = sb[TB_A0 * 32 + j];
+            const int la = __float_as_int(sb[TB_A1 * 32 + j]);
+            const float aa = sb[TB_A2 * 32 + j];
+            const float sa = sb[TB_A3 * 32 + j];
+            if (l == 0) { sb[TB_LAM * 32 + j] = __int_as_float(cl); sb[TB_ALPHA * 32 + j] = ca; }
+            if (!(ua * ca < cs)) { cl = la; ca = aa; cs = sa; amask |= 1u << j; }
+        }
+        __syncwarp();
+        // lanes beyond the batch keep the packet's wavelength (their values are never used)
+        const int mylam = l < B ? __float_as_int(sb[TB_LAM * 32 + l]) : p.lam;
+        const float mya = l < B ? sb[TB_ALPHA * 32 + l] : 1.0f;
+        const bool myab = (amask >> l) & 1u;
+        float tau = __shfl_up_sync(FULL, pol.re.tn, 1);
+        if (l == 0) tau = p.tau;
+        const float sef = tau / mya;
+
+        // 2. directions: in (before the interaction) and out (after it)
+        float kix = 0.0f, kiy = 0.0f, kiz = 0.0f, kox = 0.0f, koy = 0.0f, koz = 0.0f;
+        bool kin = false, kout = false;
+        {
+            const float ux = __shfl_up_sync(FULL, pol.ikx, 1);
+            const float uy = __shfl_up_sync(FULL, pol.iky, 1);
+            const float uz = __shfl_up_sync(FULL, pol.ikz, 1);
+            if (l == 0) { kix = p.kx; kiy = p.ky; kiz = p.kz; kin = true; }
+            else if ((amask >> (l - 1)) & 1u) { kix = ux; kiy = uy; kiz = uz; kin = true; }
+            if (myab) { kox = pol.ikx; koy = pol.iky; koz = pol.ikz; kout = true; }
+        }
+        const float mu = pol.gconst ? pol.hgmu : hg_mu(T.g[mylam], pol.re.umu);
+        // round r settles the r-th scattering of a run: the lanes that know their incoming
+        // direction rotate it, then pass their outgoing one on (B rounds at most)
+        for (int it = 0; it <= 32; ++it) {
+            if (kin && !kout) {
+                kox = kix; koy = kiy; koz = kiz;
+                mc_rotate(kox, koy, koz, mu, pol.re.cs, pol.re.sn);
+                kout = true;
+            }
+            const float vx = __shfl_up_sync(FULL, kox, 1);
+            const float vy = __shfl_up_sync(FULL, koy, 1);
+            const float vz = __shfl_up_sync(FULL, koz, 1);
+            const int pk = __shfl_up_sync(FULL, kout ? 1 : 0, 1);
+            if (!kin && l > 0 && pk) { kix = vx; kiy = vy; kiz = vz; kin = true; }
+            if (__ballot_sync(FULL, l < B && !(kin && kout)) == 0u) break;
+        }
+
+        // 3. positions before (b) and after (a) each lane's move
+        {
+            const ds mx = ds_prod(sef, kix), my = ds_prod(sef, kiy), mz = ds_prod(sef, kiz);
+            sb[TB_A0 * 32 + l] = mx.h; sb[TB_A1 * 32 + l] = mx.l;
+            sb[TB_A2 * 32 + l] = my.h; sb[TB_A3 * 32 + l] = my.l;
+            sb[TB_A4 * 32 + l] = mz.h; sb[TB_A5 * 32 + l] = mz.l;
+        }
+        __syncwarp();
+        ds X = p.x, Y = p.y, Z = p.z;
+#pragma unroll 4
+        for (int j = 0; j < B; ++j) {
+            if (l == 0) {
+                sb[TB_XH * 32 + j] = X.h; sb[TB_XL * 32 + j] = X.l;
+                sb[TB_YH * 32 + j] = Y.h; sb[TB_YL * 32 + j] = Y.l;
+                sb[TB_ZH * 32 + j] = Z.h; sb[TB_ZL * 32 + j] = Z.l;
+            }
+            X = ds_add(X, ds{sb[TB_A0 * 32 + j], sb[TB_A1 * 32 + j]});
+            Y = ds_add(Y, ds{sb[TB_A2 * 32 + j], sb[TB_A3 * 32 + j]});
+            Z = ds_add(Z, ds{sb[TB_A4 * 32 + j], sb[TB_A5 * 32 + j]});
+        }
+        __syncwarp();
+        ds bx = p.x, by = p.y, bz = p.z, ax = X, ay = Y, az = Z;
+        if (l < B) {
+            bx = ds{sb[TB_XH * 32 + l], sb[TB_XL * 32 + l]};
+            by = ds{sb[TB_YH * 32 + l], sb[TB_YL * 32 + l]};
+            bz = ds{sb[TB_ZH * 32 + l], sb[TB_ZL * 32 + l]};
+        }
+        if (l < B - 1) {
+            ax = ds{sb[TB_XH * 32 + l + 1], sb[TB_XL * 32 + l + 1]};
+            ay = ds{sb[TB_YH * 32 + l + 1], sb[TB_YL * 32 + l + 1]};
+            az = ds{sb[TB_ZH * 32 + l + 1], sb[TB_ZL * 32 + l + 1]};
+        }
+
+        // 4. wall distances, Rosseland means and jumps per lane
+        PktS pq = p;
+        pq.x = ax; pq.y = ay; pq.z = az;
+        const float Dpost = wall_distance_ds(M, W, pq);
+        float Dpre = __shfl_up_sync(FULL, Dpost, 1);
+        {
+            const float s0 = __shfl_sync(FULL, sef, 0);
+            if (!(s0 < p.dsafe) && !p.fresh) {
+                const float D0 = wall_distance_ds(M, W, p);
+                if (l == 0) Dpre = D0;
+            }
+        }
+        const unsigned below = amask & ((1u << l) - 1u);
+        const long long ut = u0 + ((long long)__popc(below) << MC_EUNIT_SHIFT);
+        float qm = q.x + 0.5f * q.y;
+        qm = qm + (ut != 0 ? (float)ut * wq : 0.0f);
+        int rj;
+        float rw;
+        mc_row_search(T.F, qm, rj, rw);
+        float aR = 0.0f;
+        aR = aR + rh * (T.kR[rj] + rw * (T.kR[rj + 1] - T.kR[rj]));
+        const float R0f = 0.999f * Dpost;
+        const bool jmp = R0f * aR >= P.mrw_gamma && R0f * mya >= P.mrw_tauthres;
+        const long long ce = (long long)p.cell_events + l + 1, nv = ne + l + 1;
+        const bool cond = P.mrw && (ce >= P.mrw_trigger ||
+                                    (P.mrw_eager_after > 0 && nv > P.mrw_eager_after));
+        const unsigned cmask = __ballot_sync(FULL, cond);
+        const unsigned jmask = __ballot_sync(FULL, jmp);
+
+        // 5. safety distance, distance bound and MRW tries
+        float dsafe = p.dsafe, dmax = p.dmax;
+        int fresh = p.fresh;
+        unsigned fmask = 0u;
+        int L = B;
+        __syncwarp();
+        sb[TB_A0 * 32 + l] = sef;
+        sb[TB_A1 * 32 + l] = Dpre;
+        sb[TB_A2 * 32 + l] = Dpost;
+        sb[TB_A3 * 32 + l] = aR;
+        __syncwarp();
+#pragma unroll 4
+        for (int j = 0; j < B; ++j) {
+            const float s = sb[TB_A0 * 32 + j];
+            const float dp = sb[TB_A1 * 32 + j];
+            const float dq = sb[TB_A2 * 32 + j];
+            const float a = sb[TB_ALPHA * 32 + j];
+            const float r = sb[TB_A3 * 32 + j];
+            if (!(s < dsafe) && !fresh) {
+                dsafe = 0.999999f * dp;
+                dmax = mc_dmax_of(dp);
+                fresh = 1;
+            }
+            const bool full = !(s < dsafe);
+            dsafe = full ? 0.0f : dsafe - s;
+            fresh = 0;
+            dmax = mc_dmax_after(dmax, s);
+            bool tried = false;
+            if (((cmask >> j) & 1u) && 0.999f * dmax * a >= P.mrw_tauthres)
+                tried = 0.999f * dmax * r >= P.mrw_gamma;
+            if (tried && ((jmask >> j) & 1u)) { L = j; break; }
+            if (tried) {
+                dsafe = 0.999999f * dq;
+                dmax = mc_dmax_of(dq);
+                fresh = 1;
+            }
+            if (full) fmask |= 1u << j;
+            if (l == 0) {
+                sb[TB_DS * 32 + j] = dsafe;
+                sb[TB_DM * 32 + j] = dmax;
+                sb[TB_FR * 32 + j] = __int_as_float(fresh);
+            }
+        }
+        __syncwarp();
+        const bool jumped = L < B;
+
+        // wall solves of the interactions whose safety distance does not suffice
+        bool cross = false, edge = false;
+        ds swd = ds{0.0f, 0.0f};
+        int wall = W_NONE;
+        float tcell = 0.0f;
+        if (((fmask >> l) & 1u) && l < L) {
+            PktS pb = p;
+            pb.x = bx; pb.y = by; pb.z = bz;
+            pb.kx = kix; pb.ky = kiy; pb.kz = kiz;
+            if (l > 0) pb.last_wall = W_NONE;
+            swd = tail_wall(M, W, pb, wall);
+            tcell = mya * swd.h;
+            if (!(tcell > tau)) cross = true;
+            else if (tau / mya > swd.h) edge = true;
+        }
+
+        // 6. exact reemission of the absorptions (own deposits known now)
+        int lamx = glam;
+        bool badg = false;
+        if (myab && l < L) {
+            const long long uo = u0 + ((long long)(__popc(below) + 1) << MC_EUNIT_SHIFT);
+            float qq = q.x + pol.rs.uq * q.y;
+            qq = qq + (float)uo * wq;
+            int j2;
+            float w2;
+            mc_row_search(T.F, qq, j2, w2);
+            const int row2 = j2 + ((pol.rs.urow < w2) ? 1 : 0);
+            if (row2 != grow) {
+                lamx = mc_cdf_search(T.cdf + (size_t)row2 * nl, nl, pol.rs.ucdf);
+                badg = lamx != glam;
+            }
+        }
+
+        // commit: the first lane that leaves the scheme decides
+        int act = 0;           // 0 continue, 1 one tail_fast_run step, 2 crossing of lane Lc
+        int Lc = L;
+        if (jumped) act = 1;
+        const unsigned abad = __ballot_sync(FULL, !(mya > 0.0f) && l < B);
+        if (abad) {
+            const int a = __ffs(abad) - 1;
+            if (a < Lc) { Lc = a; act = 1; }
+        }
+        const unsigned cb = __ballot_sync(FULL, cross || edge);
+        if (cb) {
+            const int f = __ffs(cb) - 1;
+            if (f < Lc) { Lc = f; act = ((__ballot_sync(FULL, cross) >> f) & 1u) ? 2 : 1; }
+        }
+        const unsigned gb = __ballot_sync(FULL, badg);
+        if (gb) {
+            const int s = __ffs(gb) - 1;
+            if (s + 1 <= Lc) { Lc = s + 1; act = 0; }
+        }
+        const bool late = P.late_after > 0 && ne + 1 > P.late_after;
+        int64_t* dep = late ? P.Elate : P.E;
+        if (Lc > 0) {
+            const int t = Lc - 1;
+            p.x = ds{__shfl_sync(FULL, ax.h, t), __shfl_sync(FULL, ax.l, t)};
+            p.y = ds{__shfl_sync(FULL, ay.h, t), __shfl_sync(FULL, ay.l, t)};
+            p.z = ds{__shfl_sync(FULL, az.h, t), __shfl_sync(FULL, az.l, t)};
+            p.kx = __shfl_sync(FULL, kox, t);
+            p.ky = __shfl_sync(FULL, koy, t);
+            p.kz = __shfl_sync(FULL, koz, t);
+            p.tau = __shfl_sync(FULL, pol.re.tn, t);
+            const int lx = __shfl_sync(FULL, lamx, t);
+            const int lm = __shfl_sync(FULL, mylam, t);
+            p.lam = ((amask >> t) & 1u) ? lx : lm;
+            p.dsafe = sb[TB_DS * 32 + t];
+            p.dmax = sb[TB_DM * 32 + t];
+            p.fresh = __float_as_int(sb[TB_FR * 32 + t]);
+            p.cell_events += Lc;
+            p.nevents += Lc;
+            p.last_wall = W_NONE;
+            const unsigned cm = (Lc == 32) ? FULL : ((1u << Lc) - 1u);
+            const int A = __popc(amask & cm);
+            cnt.events += Lc;
+            cnt.absorb += A;
+            cnt.scatter += Lc - A;
+            if (late) cnt.late += Lc;
+            if (A > 0) {
+                const long long units = (long long)A << MC_EUNIT_SHIFT;
+                if (l == 0) atomicAdd((unsigned long long*)(dep + base + c), (unsigned long long)units);
+                pol.own_add(c, units);
+            }
+            steps += Lc;
+        }
+        if (act == 2) {
+            // crossing of lane Lc: its wall solve at the committed position and direction
+            const ds sw = ds{__shfl_sync(FULL, swd.h, Lc), __shfl_sync(FULL, swd.l, Lc)};
+            const int wl = __shfl_sync(FULL, wall, Lc);
+            const float tc2 = __shfl_sync(FULL, tcell, Lc);
+            p.x = ds_move2(p.x, sw, p.kx);
+            p.y = ds_move2(p.y, sw, p.ky);
+            p.z = ds_move2(p.z, sw, p.kz);
+            p.tau = p.tau - tc2;
+            p.dsafe = 0.0f;
+            p.dmax = MC_DMAX_UNKNOWN;
+            p.fresh = 1;
+            p.ncross += 1;
+            cnt.crossings += 1;
+            p.cell_events = 0;
+            steps += 1;
+            switch (wl) {
+                case W_ROUT:
+                    p.ir += 1;
+                    p.last_wall = W_RIN;
+                    if (p.ir >= M.nr) {
+                        cnt.escaped += 1;
+                        if (P.escape && l == 0)
+                            atomicAdd((unsigned long long*)(P.escape + (int64_t)p.m * nl + p.lam), 1ull);
+                        return 2;
+                    }
+                    break;
+                case W_RIN: p.ir -= 1; p.last_wall = W_ROUT; break;
+                case W_TLO: p.itv -= 1; p.last_wall = W_THI; break;
+                case W_THI: p.itv += 1; p.last_wall = W_TLO; break;
+                case W_PLO: p.ip = (p.ip == 0) ? M.np - 1 : p.ip - 1; p.last_wall = W_PHI; break;
+                case W_PHI: p.ip = (p.ip == M.np - 1) ? 0 : p.ip + 1; p.last_wall = W_PLO; break;
+                default: cnt.killed += 1; return 2;
+            }
+            if (p.ncross > 100000000) {
+                cnt.killed += 1;
+                return 2;
+            }
+        } else if (act == 1) {
+            int s1 = 0;
+            const int r = tail_fast_run(p, P, M, T, cnt, pol, tc, 1, s1);
+            steps += s1;
+            if (r != 1) return r;
+        }
+        bcap = (act == 0 && Lc == B) ? 32 : 16;
+    }
+    return 1;
+}
+
 // Continuation of parked packets: one packet per warp (WarpPol), taken from a queue.
 template <int NS, class G>
 __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
@@ -1527,11 +1934,16 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
         if (lane == 0) live = model_live(P, p.m) ? 1 : 0;
         bool alive = __shfl_sync(0xffffffffu, live, 0) != 0;
         TailCell tc;
+        float* tsb = nullptr;
+        if constexpr (NS == 1 && std::is_same<G, GeoS>::value) {
+            __shared__ float s_tail[(MC_TAIL_SMEM / 4)];
+            tsb = s_tail + (threadIdx.x >> 5) * (TB_NF * 32);
+        }
         while (alive) {
             if constexpr (NS == 1 && std::is_same<G, GeoS>::value) {
                 // fast steps up to the next periodic check, then one general step
                 int nfast = 0;
-                const int r = tail_fast_run(p, P, Mw, T, cnt, pol, tc, 4096 - (int)(iter & 4095u),
+                const int r = tail_batch_run(p, P, Mw, T, cnt, pol, tc, tsb, 4096 - (int)(iter & 4095u),
                                             nfast);
                 iter += (unsigned)nfast;
                 if (r == 0) alive = mc_step<NS, WarpPol, G>(p, P, Mw, T, cnt, pol);
@@ -1991,7 +2403,8 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     // per-thread own-deposit caches of the per-thread transport launches
     size_t own_bytes = (size_t)P->block * MC_OWN * (sizeof(int) + sizeof(long long)) +
                        (size_t)P->block * sizeof(int);
-    P->smem_tables = (dust_bytes + cum_bytes + own_bytes + 64) <= (size_t)smem_max;
+    // (the continuation kernel's static staging of batched walks comes on top)
+    P->smem_tables = (dust_bytes + cum_bytes + own_bytes + MC_TAIL_SMEM + 64) <= (size_t)smem_max;
     P->smem_bytes = (P->smem_tables ? dust_bytes : 0) + cum_bytes + own_bytes + 16;
     // workspace layout
     size_t o = 0;
