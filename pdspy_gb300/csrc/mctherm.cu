@@ -1608,8 +1608,13 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
             const int la = __float_as_int(sb[TB_A1 * 32 + j]);
             const float aa = sb[TB_A2 * 32 + j];
             const float sa = sb[TB_A3 * 32 + j];
-            if (l == 0) { sb[TB_LAM * 32 + j] = __int_as_float(cl); sb[TB_ALPHA * 32 + j] = ca; }
-            if (!(ua * ca < cs)) { cl = la; ca = aa; cs = sa; amask |= 1u << j; }
+            sb[TB_LAM * 32 + j] = __int_as_float(cl);   // every lane stores the same value
+            sb[TB_ALPHA * 32 + j] = ca;
+            const bool ab = !(ua * ca < cs);
+            cl = ab ? la : cl;
+            ca = ab ? aa : ca;
+            cs = ab ? sa : cs;
+            amask |= (unsigned)ab << j;
         }
         __syncwarp();
         // lanes beyond the batch keep the packet's wavelength (their values are never used)
@@ -1659,11 +1664,9 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
         ds X = p.x, Y = p.y, Z = p.z;
 #pragma unroll 4
         for (int j = 0; j < B; ++j) {
-            if (l == 0) {
-                sb[TB_XH * 32 + j] = X.h; sb[TB_XL * 32 + j] = X.l;
-                sb[TB_YH * 32 + j] = Y.h; sb[TB_YL * 32 + j] = Y.l;
-                sb[TB_ZH * 32 + j] = Z.h; sb[TB_ZL * 32 + j] = Z.l;
-            }
+            sb[TB_XH * 32 + j] = X.h; sb[TB_XL * 32 + j] = X.l;
+            sb[TB_YH * 32 + j] = Y.h; sb[TB_YL * 32 + j] = Y.l;
+            sb[TB_ZH * 32 + j] = Z.h; sb[TB_ZL * 32 + j] = Z.l;
             X = ds_add(X, ds{sb[TB_A0 * 32 + j], sb[TB_A1 * 32 + j]});
             Y = ds_add(Y, ds{sb[TB_A2 * 32 + j], sb[TB_A3 * 32 + j]});
             Z = ds_add(Z, ds{sb[TB_A4 * 32 + j], sb[TB_A5 * 32 + j]});
@@ -1728,30 +1731,23 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
             const float dq = sb[TB_A2 * 32 + j];
             const float a = sb[TB_ALPHA * 32 + j];
             const float r = sb[TB_A3 * 32 + j];
-            if (!(s < dsafe) && !fresh) {
-                dsafe = 0.999999f * dp;
-                dmax = mc_dmax_of(dp);
-                fresh = 1;
-            }
+            // selects rather than branches: the same values, a shorter dependent chain
+            const bool rf = !(s < dsafe) && !fresh;
+            dsafe = rf ? 0.999999f * dp : dsafe;
+            dmax = rf ? mc_dmax_of(dp) : dmax;
             const bool full = !(s < dsafe);
             dsafe = full ? 0.0f : dsafe - s;
-            fresh = 0;
             dmax = mc_dmax_after(dmax, s);
-            bool tried = false;
-            if (((cmask >> j) & 1u) && 0.999f * dmax * a >= P.mrw_tauthres)
-                tried = 0.999f * dmax * r >= P.mrw_gamma;
+            const bool c1 = ((cmask >> j) & 1u) && 0.999f * dmax * a >= P.mrw_tauthres;
+            const bool tried = c1 && 0.999f * dmax * r >= P.mrw_gamma;
             if (tried && ((jmask >> j) & 1u)) { L = j; break; }
-            if (tried) {
-                dsafe = 0.999999f * dq;
-                dmax = mc_dmax_of(dq);
-                fresh = 1;
-            }
-            if (full) fmask |= 1u << j;
-            if (l == 0) {
-                sb[TB_DS * 32 + j] = dsafe;
-                sb[TB_DM * 32 + j] = dmax;
-                sb[TB_FR * 32 + j] = __int_as_float(fresh);
-            }
+            dsafe = tried ? 0.999999f * dq : dsafe;
+            dmax = tried ? mc_dmax_of(dq) : dmax;
+            fresh = tried ? 1 : 0;
+            fmask |= (unsigned)full << j;
+            sb[TB_DS * 32 + j] = dsafe;
+            sb[TB_DM * 32 + j] = dmax;
+            sb[TB_FR * 32 + j] = __int_as_float(fresh);
         }
         __syncwarp();
         const bool jumped = L < B;
