@@ -114,6 +114,11 @@ def walker_models(n=64, seed=0, g=0.6, scale=1.0):
     return out
 
 
+def walker_model(i, n=64, seed=0, g=0.6):
+    """Walker i of walker_models(n, seed)."""
+    return walker_models(n=n, seed=seed, g=g)[i]
+
+
 def spiral_disk(nr=128, ntheta=128, nphi=128, phase=0.0, mass=1e-3, rout=100.0, h0=0.1,
                 plh=1.25, plrho=2.25, pitch_deg=15.0, amp=0.3, large_fraction=0.9, g=0.6):
     """3-D disk with a two-armed logarithmic spiral, small grains at h and large grains

@@ -50,3 +50,18 @@ def test_config0_epoch_matches_sequential_per_cell():
     assert np.median(np.abs(z)) < 0.8
     assert np.mean(np.abs(z) > 3.0) < 0.015
     assert abs(np.mean(z)) < 0.3
+
+
+@pytest.mark.slow
+def test_heavy_walker_epoch_matches_sequential_per_cell():
+    """Walker 36 of the batched workload (one of the walkers with the longest walks: dense
+    inner rim, walks of 1e7-1e8 interactions in both forms), 1e4 packets, production MRW and
+    schedule, 16 seeds of each form: every cell crossed >= 1e3 times per run within 4 sigma."""
+    seeds = range(16)
+    E, C = _cases.oracle_ensemble("walker_model", {"i": 36}, 10000, seeds, **MRW)
+    S, _ = _cases.oracle_ensemble("walker_model", {"i": 36}, 10000, [1000 + s for s in seeds],
+                                  sequential=True, **MRW)
+    z, rel = _cases.four_sigma(E, S, C)
+    assert z.size >= 30
+    assert np.all(np.abs(z) < 4.0), np.abs(z).max()
+    assert np.median(np.abs(z)) < 1.0
