@@ -660,9 +660,9 @@ def main():
                 os.cpu_count(), dt)}
 
     K, P = plan.opts.nepoch, plan.opts.npilot
-    # start + (prep + transport) per pass and epoch + two continuation launches +
-    # temperature + finish
-    launches_per_step = 2 * st["launches"] + 1
+    # start + a prep per pass and epoch + the transport launches (each pass and epoch, its
+    # drained walks one per warp, the two continuation launches) + temperature + finish
+    launches_per_step = st["launches"] + K + P + 3
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup,

@@ -95,8 +95,10 @@ struct McParams {
     const ParkRec* park_in;      // phases 1 and 2: the packets to resume
     const unsigned long long* park_in_count;
     int64_t park_in_cap;
-    unsigned long long* inflight;   // phase 1: packets taken and not yet finished
-    int64_t drain_below;         // phase 1: drain when fewer are in flight (0 = never)
+    unsigned long long* inflight;   // packets taken and not yet finished (when draining)
+    int64_t drain_below;         // drain when fewer are in flight (0 = never)
+    ParkRec* drain_out;          // drained packets, resumed one per warp
+    unsigned long long* drain_out_count;
     int32_t pilot;               // pilot pass: packets stop after late_after events
     int32_t phase;               // 0: epoch launch; 1: parked packets, one per thread;
                                  // 2: drained packets, one per warp
@@ -429,6 +431,7 @@ struct LanePol {
     }
     __device__ __forceinline__ float cached_value(int) const { return 0.0f; }
     __device__ __forceinline__ bool leader() const { return true; }
+    __device__ __forceinline__ unsigned long long bcast(unsigned long long v) const { return v; }
     // densities of cell c (rho0 = the model's [spec][cell] block)
     template <int NS>
     __device__ __forceinline__ void density(const float* rho0, int ncell, int, int c, float* rh) {
@@ -676,6 +679,10 @@ struct WarpPol {
     }
     __device__ __forceinline__ float cached_value(int k) const { return cval[k]; }
     __device__ __forceinline__ bool leader() const { return lane == 0; }
+    // lane 0's value in every lane
+    __device__ __forceinline__ unsigned long long bcast(unsigned long long v) const {
+        return __shfl_sync(0xffffffffu, v, 0);
+    }
     // densities, q per deposit unit and snapshots of the packet's cell, reloaded when the
     // cell changes
     int dm = -1, dc = -1, qm = -1, qc = -1, qe = -1, wm = -1, wc = -1;
@@ -1032,11 +1039,15 @@ __device__ __forceinline__ bool mc_step(typename G::Pkt& p, const McParams& P, c
         }
         if (P.late_after > 0 && p.nevents == P.late_after && P.phase == 0) {
             if (P.pilot) return false;   // later deposits of pilot packets are discarded
-            unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
+            unsigned long long slot = 0;
+            if (pol.leader()) slot = atomicAdd(P.park_out_count, 1ull);
+            slot = pol.bcast(slot);
             if ((long long)slot < P.park_out_cap) {
-                ParkRec r;
-                park_save<G>(r, p, pol);
-                P.park_out[slot] = r;
+                if (pol.leader()) {
+                    ParkRec r;
+                    park_save<G>(r, p, pol);
+                    P.park_out[slot] = r;
+                }
                 cnt.parked += 1;
                 return false;
             }
@@ -1190,7 +1201,7 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
                     got = live;
                 }
             }
-            if (P.phase == 1) {
+            if (P.drain_below > 0) {
                 int ng = __popc(__ballot_sync(0xffffffffu, got));
                 if (lane == 0 && ng) atomicAdd(P.inflight, (unsigned long long)ng);
             }
@@ -1206,11 +1217,12 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
             active = mc_step<NS, LanePol, G>(p, P, P.models[p.m], T, cnt, lanepol);
             if (!active && p.nevents > cnt.maxev) cnt.maxev = p.nevents;
         }
-        if (P.phase == 1) {
+        if (P.drain_below > 0) {
             int nf = __popc(__ballot_sync(0xffffffffu, was && !active));
             if (lane == 0 && nf) atomicAdd(P.inflight, (unsigned long long)(-(long long)nf));
-            // few packets left: hand them to the warp-per-packet launch
-            if (!queue_open && P.drain_below > 0 && (iter & 63u) == 63u) {
+            // few packets left: hand them to the warp-per-packet launch (an epoch's walks
+            // resume there with the epoch's snapshot and still park at late_after)
+            if (!queue_open && (iter & 63u) == 63u) {
                 int dr = 0;
                 if (lane == 0)
                     dr = (long long)*(volatile unsigned long long*)P.inflight < P.drain_below;
@@ -1218,11 +1230,11 @@ __global__ void __launch_bounds__(256, 2) mc_transport_kernel(McParams P) {
                 if (dr) {
                     bool parked = false;
                     if (active) {
-                        unsigned long long slot = atomicAdd(P.park_out_count, 1ull);
+                        unsigned long long slot = atomicAdd(P.drain_out_count, 1ull);
                         if ((long long)slot < P.park_out_cap) {
                             ParkRec r;
                             park_save<G>(r, p, lanepol);
-                            P.park_out[slot] = r;
+                            P.drain_out[slot] = r;
                             parked = true;
                             active = false;
                             cnt.drained += 1;
@@ -1329,6 +1341,8 @@ __device__ __forceinline__ int tail_fast_run(PktS& p, const McParams& P, const M
         alpha = alpha + rh * T.kext[p.lam];
         if (!(alpha > 0.0f)) return 0;
         if (p.nevents + 1 >= P.max_inter) return 0;
+        // a walk resumed within its epoch parks at late_after: mc_step takes that step
+        if (P.phase == 0 && P.late_after > 0 && p.nevents + 1 >= P.late_after) return 0;
         const float sef = p.tau / alpha;
         if (!(sef < p.dsafe) && !p.fresh) {
             const float D = wall_distance_ds(M, W, p);
@@ -1545,6 +1559,9 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
         const long long ne = p.nevents;
         if (P.late_after > 0 && ne < P.late_after && ne + B > P.late_after)
             B = (int)(P.late_after - ne);
+        // within an epoch the late_after-th interaction (which parks) is left to mc_step
+        if (P.phase == 0 && P.late_after > 0 && ne + B >= P.late_after)
+            B = (int)(P.late_after - ne - 1);
         bool ok = p.ir >= 0 && B >= 1 && ne + B < (long long)P.max_inter;
         if (ok) {
             if (p.ir != tc.ir || p.itv != tc.itv || p.ip != tc.ip || p.epoch != tc.epoch) {
@@ -1977,8 +1994,9 @@ __global__ void __launch_bounds__(256) mc_continue_kernel(McParams P) {
                                 cnt.scatter, cnt.mrw, cnt.late, cnt.parked};
         const int slot[9] = {ST_KILLED, ST_ESCAPED, ST_CROSSINGS, ST_EVENTS, ST_ABSORB, ST_SCATTER,
                              ST_MRW, ST_LATE, ST_PARKED};
-        for (int i = 0; i < 9; ++i)
-            if (v[i]) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)v[i]);
+        if (P.count_stats)
+            for (int i = 0; i < 9; ++i)
+                if (v[i]) atomicAdd((unsigned long long*)(P.stats + slot[i]), (unsigned long long)v[i]);
         int64_t* L = P.stats + MC_LSTAT + MC_LSTRIDE * P.lslot;
         atomicMax((unsigned long long*)(L + 1), (unsigned long long)globaltimer());
         atomicMax((unsigned long long*)(L + 2), (unsigned long long)cnt.maxev);
@@ -2123,6 +2141,8 @@ struct pdgpu_mc_plan {
     float g0;
     int64_t park_cap;
     int nqueue;
+    bool epoch_drain;   // the last walks of each epoch launch resume one per warp
+    int nlaunch;        // launches of the last run
     int device, nsm, block, grid;
     bool smem_tables;
     size_t smem_bytes;
@@ -2432,7 +2452,9 @@ pdgpu_status pdgpu_mc_plan_create(int32_t nmodels, const pdgpu_model_desc* model
     P->ws_mdl = place((size_t)nmodels * sizeof(int64_t));
     P->ws_mstat = place((size_t)nmodels * sizeof(int32_t));
     P->use_mdl = false;
-    P->nqueue = P->K + P->npilot + 2;   // one work counter per launch
+    // with draining, every pilot and epoch launch is followed by a warp-per-packet launch
+    P->epoch_drain = P->opt.drain_below >= 0 && 2 * (P->K + P->npilot) + 2 <= MC_MAX_LAUNCH;
+    P->nqueue = (P->epoch_drain ? 2 : 1) * (P->K + P->npilot) + 2;   // one work counter per launch
     P->ws_queue = place((size_t)P->nqueue * sizeof(unsigned long long));
     P->ws_total = (o + 255) / 256 * 256;
     P->uploaded_ws = nullptr;
@@ -2564,16 +2586,21 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     unsigned long long* counts = (unsigned long long*)(w + P->ws_parkcnt);
     ParkRec* listA = (ParkRec*)(w + P->ws_park);
     ParkRec* listB = (ParkRec*)(w + P->ws_park2);
-    prm.park_out = phase == 0 ? listA : listB;
-    prm.park_out_count = phase == 0 ? counts : counts + 1;
+    // phase 3: the packets drained from an epoch launch (list B), resumed one per warp with
+    // the epoch's semantics (phase 0: deposits to the epoch's target, parking in list A)
+    const int sem = phase == 3 ? 0 : phase;
+    prm.park_out = (phase == 0 || phase == 3) ? listA : listB;
+    prm.park_out_count = (phase == 0 || phase == 3) ? counts : counts + 1;
     prm.park_out_cap = P->park_cap;
     prm.park_in = phase == 1 ? listA : listB;
     prm.park_in_count = phase == 1 ? counts : counts + 1;
     prm.park_in_cap = P->park_cap;
+    prm.drain_out = listB;
+    prm.drain_out_count = counts + 1;
     prm.inflight = counts + 2;
     prm.drain_below = 0;
     prm.pilot = final_pass ? 0 : 1;
-    prm.phase = phase;
+    prm.phase = sem;
     prm.lslot = lslot;
     prm.escape = final_pass ? (int64_t*)(w + P->ws_escape) : nullptr;
     prm.stats = (int64_t*)(w + P->ws_stats);
@@ -2584,7 +2611,7 @@ static pdgpu_status launch_transport(pdgpu_mc_plan* P, char* w, const float* rho
     prm.mstat = (int32_t*)(w + P->ws_mstat);
     prm.use_mdl = P->use_mdl ? 1 : 0;
     prm.total = phase == 0 ? P->cum[(size_t)epoch * (P->nm + 1) + P->nm] : P->park_cap;
-    if (phase == 1 && P->opt.drain_below >= 0) {
+    if ((phase == 1 || (phase == 0 && P->epoch_drain)) && P->opt.drain_below >= 0) {
         int64_t d = P->opt.drain_below;
         if (d == 0) {
             // as many packets as the warp-per-packet launch keeps running at once
@@ -2712,27 +2739,41 @@ pdgpu_status pdgpu_mc_plan_run(pdgpu_mc_plan* P, const float* rho, double* tempe
     pdgpu_status rc;
     int lslot = 0;
     P->ev_used = 0;
+    unsigned long long* counts = (unsigned long long*)(w + P->ws_parkcnt);
+    // one pilot or epoch launch; with draining, its last walks then resume one per warp
+    auto epoch_launch = [&](int64_t* target, int epoch, uint32_t tag, bool final_pass) -> pdgpu_status {
+        if (P->epoch_drain &&
+            cudaMemsetAsync(counts + 1, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess)
+            return PDGPU_CUDA_ERROR;
+        pdgpu_status r = launch_transport(P, w, rho, target, epoch, tag, lslot++, final_pass, 0, st);
+        if (r == PDGPU_OK && P->epoch_drain)
+            r = launch_transport(P, w, rho, target, epoch, tag, lslot++, final_pass, 3, st);
+        return r;
+    };
     // first epoch: pilot passes write D (and stop at late_after), the real pass writes E
     for (int pass = P->npilot; pass >= 0; --pass) {
         if ((rc = launch_prep(P, w, rho, D, 1, 0, st)) != PDGPU_OK) return rc;
         if (pass > 0) {
             if (cudaMemsetAsync(D, 0, cells_bytes, st) != cudaSuccess) return PDGPU_CUDA_ERROR;
-            rc = launch_transport(P, w, rho, D, 0, (uint32_t)pass, lslot++, false, 0, st);
+            rc = epoch_launch(D, 0, (uint32_t)pass, false);
         } else {
-            rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 0, st);
+            rc = epoch_launch(E, 0, 0u, true);
         }
         if (rc != PDGPU_OK) return rc;
     }
     for (int k = 1; k < P->K; ++k) {
         if ((rc = launch_prep(P, w, rho, E, 0, k, st)) != PDGPU_OK) return rc;
-        if ((rc = launch_transport(P, w, rho, E, k, 0u, lslot++, true, 0, st)) != PDGPU_OK) return rc;
+        if ((rc = epoch_launch(E, k, 0u, true)) != PDGPU_OK) return rc;
     }
     // packets parked after late_after events finish here, each with its epoch's snapshot:
     // one per thread while there are many, the last few one per warp
     if (P->opt.late_after > 0) {
+        if (cudaMemsetAsync(counts + 1, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess)
+            return PDGPU_CUDA_ERROR;
         if ((rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 1, st)) != PDGPU_OK) return rc;
         if ((rc = launch_transport(P, w, rho, E, 0, 0u, lslot++, true, 2, st)) != PDGPU_OK) return rc;
     }
+    P->nlaunch = lslot;
     TempParams tp;
     tp.models = (const McModel*)(w + P->ws_models);
     tp.dpool = (const double*)(w + P->ws_dpool);
@@ -2768,7 +2809,7 @@ pdgpu_status pdgpu_mc_plan_stats(pdgpu_mc_plan* P, const void* ws, void* stream,
     S->scatterings = h[ST_SCATTER];
     S->mrw_steps = h[ST_MRW];
     S->status = (int32_t)h[ST_STATUS];
-    S->launches = P->K + P->npilot + (P->opt.late_after > 0 ? 2 : 0);
+    S->launches = P->nlaunch;
     S->parked = h[ST_PARKED];
     S->drained = h[ST_DRAINED];
     S->late_units = h[ST_LATE];
