@@ -541,7 +541,7 @@ def main():
             launch_counts.append(plan.launch_counts())
             stats.append(plan.check_status())
 
-    # per step: the warp-per-packet stage (the last transport launch: the longest walks) and
+    # per step: the warp-per-packet stage (the last launch: the longest walks) and
     # everything before it
     tail_ms = [lm[-1] if lm else 0.0 for lm in launch_ms]
     bulk_ms = [a - b for a, b in zip(step_ms, tail_ms)]
@@ -625,7 +625,9 @@ def main():
     if l2 and t_bulk_k > 0:
         ab = sum(alg(d) for d in bulk) / t_bulk_k / 1e9
         at = sum(d["deposits"] for d in bulk) / t_bulk_k
-        roofline["bulk"] = {"kernel": "mc_transport_kernel (epoch and first continuation launches)",
+        roofline["bulk"] = {"kernel": "mc_transport_kernel (pilot, epoch and first continuation "
+                                      "launches) with the epochs' drained walks "
+                                      "(mc_continue_kernel)",
                             "l2_achieved_gbs": ab, "l2_peak_gbs": l2["copy_gbs"],
                             "l2_frac": ab / l2["copy_gbs"], "atomics_per_s": at,
                             "atomic_peak_per_s": l2["red_per_s"],
