@@ -122,9 +122,10 @@ typedef struct {
     int32_t fp64_walls;             /* 0: double-single positions and wall roots (FP32  */
                                     /* pipe, default); 1: the same kernels with FP64    */
                                     /* geometry, the precision reference                */
-    int64_t drain_below;            /* resumed packets run one per thread until fewer   */
-                                    /* than this many are left, then one per warp       */
-                                    /* (0 = the warp launch's width, -1 = never)        */
+    int64_t drain_below;            /* the packets of each pilot, epoch and resumed-    */
+                                    /* packet launch run one per thread until fewer than */
+                                    /* this many are left, then one per warp (0 = the    */
+                                    /* warp launch's width, -1 = never)                  */
 } pdgpu_mc_options;
 
 typedef struct {
