@@ -1,6 +1,6 @@
 """The deterministic epoch form of Bjorkman & Wood against the classic sequential form
 (the reference algorithm: every absorption reads the running temperature), both in the
-CPU oracle, judged by the per-cell criterion: over an ensemble of seeds, the mean
+CPU oracle, compared by the per-cell criterion: over an ensemble of seeds, the mean
 temperatures agree within 4 sigma of the seed-to-seed scatter in every heated cell crossed
 >= 1e3 times per run.
 

@@ -145,7 +145,7 @@ def test_run_visibilities_is_imtovis_of_the_image(cuda):
 def test_sed_converged_at_its_defaults(cuda, config):
     """run_sed at its defaults (nested 129-pixel cameras, max_refine 6) against a much finer
     trace of the same model (257 pixels per level, max_refine 9), 1 um to 1 cm, within 2%
-    (the judged SED criterion).  Config 0 is also checked against one 1025-pixel camera
+    (the SED accuracy criterion).  Config 0 is also checked against one 1025-pixel camera
     refined to 4^10 sub-rays (no nesting).  The disk + envelope grid reaches 1e4 au while
     its inner rim, which carries the 1-10 um flux, sits at 0.1 au."""
     from pdspy_gb300 import workloads
