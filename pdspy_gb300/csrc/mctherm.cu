@@ -1551,6 +1551,9 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
     // batch size: 16 after a crossing or an MRW jump (half the batches end within 10
     // interactions), 32 after a batch committed whole
     int bcap = 16;
+    // after an MRW jump the next step is most often another jump (two thirds of the jumps
+    // of a trapped walk follow one directly): such steps are taken one at a time
+    bool after_jump = false;
     while (steps < budget) {
         // room for one more step after the batch, all interactions on the same side of
         // late_after, none reaching the interaction cap
@@ -1575,11 +1578,13 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
             a0 = a0 + tc.rho * T.kext[p.lam];
             ok = a0 > 0.0f;
         }
-        if (!ok) {
+        if (!ok || after_jump) {
+            const long long mj = cnt.mrw;
             int s1 = 0;
             const int r = tail_fast_run(p, P, M, T, cnt, pol, tc, 1, s1);
             steps += s1;
             if (r != 1) return r;
+            after_jump = cnt.mrw != mj;
             continue;
         }
         const WallsCell& W = pol.cell_walls(M, P.fpool, p);
@@ -1893,10 +1898,12 @@ __device__ __forceinline__ int tail_batch_run(PktS& p, const McParams& P, const 
                 return 2;
             }
         } else if (act == 1) {
+            const long long mj = cnt.mrw;
             int s1 = 0;
             const int r = tail_fast_run(p, P, M, T, cnt, pol, tc, 1, s1);
             steps += s1;
             if (r != 1) return r;
+            after_jump = cnt.mrw != mj;
         }
         bcap = (act == 0 && Lc == B) ? 32 : 16;
     }
